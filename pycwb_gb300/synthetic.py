@@ -1,0 +1,79 @@
+"""Seeded synthetic clusters with the shapes of the sky-scan workloads.
+
+No detector data, WDM library or injection package is available offline,
+so the td-amplitude blocks that the sky scan consumes are drawn directly:
+
+* td00/td90: (2K+1, nIFO, n_pix) float32, unit-variance Gaussian noise plus
+  a coherent signal of a chosen network SNR projected from one sky
+  direction ``l_true``.  The signal sits at delay index ml[i, l_true] + K of
+  each detector and leaks into neighbouring delay samples with a Gaussian
+  profile (width 1.5 samples), which mimics the time-delay filter response.
+* rms: (n_pix, nIFO) float32 normalised inverse-noise weights
+  r_i = s_i^-1 / sqrt(sum_k s_k^-2) with per-detector noise s ~ U[0.5, 2],
+  the normalisation of pycwb/modules/likelihoodWP/pixel_data.py:60-62.
+
+``regulators`` derives the per-segment constants exactly as
+pycwb/modules/likelihoodWP/likelihood_setup.py:133-147 does.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def regulators(n_ifo, acore=math.sqrt(2.0), gamma=0.5, delta=0.5, netCC=0.5, netRHO=0.0):
+    """Segment constants from the analysis config (likelihood_setup.py:133-147)."""
+    network_energy_threshold = 2 * acore * acore * n_ifo
+    gamma_regulator = gamma * gamma * 2 / 3
+    if delta == 0.0:
+        delta = 0.00001
+    delta_regulator = abs(delta) if abs(delta) < 1 else 1
+    return dict(network_energy_threshold=network_energy_threshold,
+                gamma_regulator=gamma_regulator, delta_regulator=delta_regulator,
+                netCC=float(netCC), net_rho_threshold=abs(netRHO),
+                netEC_threshold=abs(netRHO) * abs(netRHO) * 2)
+
+
+def make_rms(rng, n_pix, n_ifo):
+    sigma = rng.uniform(0.5, 2.0, size=(n_ifo, n_pix))
+    inv = 1.0 / sigma
+    norm = 1.0 / np.sqrt(np.sum(inv ** 2, axis=0))
+    return np.ascontiguousarray((inv * norm[np.newaxis, :]).astype(np.float32).T)
+
+
+def make_cluster(rng, ml, FP_t, FX_t, n_pix, K, snr, l_true=None, spread=1.5):
+    """One synthetic cluster; returns (td00, td90, rms, l_true)."""
+    n_ifo, n_sky = ml.shape
+    D = 2 * K + 1
+    if l_true is None:
+        l_true = int(rng.integers(n_sky))
+    rms = make_rms(rng, n_pix, n_ifo)
+    td00 = rng.standard_normal((D, n_ifo, n_pix), dtype=np.float32)
+    td90 = rng.standard_normal((D, n_ifo, n_pix), dtype=np.float32)
+
+    w = np.exp(rng.standard_normal(n_pix))
+    w /= w.sum()
+    h = rng.standard_normal((4, n_pix)) * np.sqrt(w)[None, :]   # hp00, hx00, hp90, hx90
+    fp = FP_t[l_true].astype(np.float64)
+    fx = FX_t[l_true].astype(np.float64)
+    r = rms.astype(np.float64)                                   # (n_pix, n_ifo)
+    s00 = r * (fp[None, :] * h[0][:, None] + fx[None, :] * h[1][:, None])
+    s90 = r * (fp[None, :] * h[2][:, None] + fx[None, :] * h[3][:, None])
+    e = float(np.sum(s00 ** 2 + s90 ** 2))
+    if e > 0.0:
+        scale = snr / math.sqrt(e)
+        s00 *= scale
+        s90 *= scale
+    d = np.arange(D)
+    for i in range(n_ifo):
+        d0 = int(ml[i, l_true]) + K
+        prof = np.exp(-0.5 * ((d - d0) / spread) ** 2)[:, None]
+        td00[:, i, :] += (prof * s00[:, i][None, :]).astype(np.float32)
+        td90[:, i, :] += (prof * s90[:, i][None, :]).astype(np.float32)
+    return td00, td90, rms, l_true
+
+
+def log_uniform_sizes(rng, n, lo, hi):
+    return np.exp(rng.uniform(math.log(lo), math.log(hi), size=n)).astype(np.int64)

@@ -1,0 +1,227 @@
+"""Generate golden input/output vectors by running PycWB's own kernels.
+
+The reference's hot-path kernel files import only numpy, math and numba:
+
+* pycwb/modules/likelihoodWP/dpf.py       (calculate_dpf, dpf_np_loops_vec)
+* pycwb/modules/likelihoodWP/sky_stat.py  (load_data_from_td, avx_GW_ps, ...)
+* pycwb/modules/likelihoodWP/sky_scan.py  (scan_sky_for_best_fit)
+* pycwb/utils/td_vector_kernels.py        (batch_get_td_vecs)
+
+numba is not installed here, so this script installs a small stand-in
+module under the name ``numba``: ``njit`` returns the Python function,
+``prange`` is ``range``, ``vectorize`` casts scalar arguments and the result
+to the declared signature, and the type objects (``float32`` ...) construct
+NumPy scalars and carry a ``.dtype``.  The reference files are then loaded
+unmodified by file path and executed with NumPy scalar semantics.  The
+outputs are written as ``.npz`` fixtures next to this script.
+
+Usage (needs the reference checkout; not used at test time)::
+
+    python tests/golden/make_golden.py /path/to/pycwb-reference
+"""
+
+from __future__ import annotations
+
+import importlib.util
+import math
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+
+# --------------------------------------------------------------------------
+# numba stand-in
+# --------------------------------------------------------------------------
+class _NbType:
+    def __init__(self, np_type):
+        self.np_type = np_type
+        self.dtype = np.dtype(np_type)
+
+    def __call__(self, *args):
+        if args and all(isinstance(a, _NbType) for a in args):
+            return (self, args)  # a signature: (return type, argument types)
+        return self.np_type(*args)
+
+    def __getitem__(self, item):  # array type spelling, e.g. float32[:]
+        return self
+
+
+def _install_numba_stub():
+    nb = types.ModuleType("numba")
+
+    def njit(*args, **kwargs):
+        if len(args) == 1 and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda f: f
+
+    def vectorize(sigs, **kwargs):
+        ret_t, arg_ts = sigs[0]
+
+        def deco(f):
+            def wrapped(*a):
+                cast = [t.np_type(x) for t, x in zip(arg_ts, a)]
+                return ret_t.np_type(f(*cast))
+            return wrapped
+        return deco
+
+    def guvectorize(sigs, layout, **kwargs):
+        return lambda f: f
+
+    nb.njit = njit
+    nb.jit = njit
+    nb.vectorize = vectorize
+    nb.guvectorize = guvectorize
+    nb.prange = range
+    for name, t in (("float32", np.float32), ("float64", np.float64),
+                    ("int32", np.int32), ("int64", np.int64),
+                    ("uint32", np.uint32)):
+        setattr(nb, name, _NbType(t))
+    sys.modules["numba"] = nb
+
+
+def _load(name, path, package=None):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    if package:
+        mod.__package__ = package
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_reference(ref_root):
+    _install_numba_stub()
+    lwp = os.path.join(ref_root, "pycwb", "modules", "likelihoodWP")
+    pkg = types.ModuleType("ref_lwp")
+    pkg.__path__ = [lwp]
+    sys.modules["ref_lwp"] = pkg
+    dpf = _load("ref_lwp.dpf", os.path.join(lwp, "dpf.py"), "ref_lwp")
+    stat = _load("ref_lwp.sky_stat", os.path.join(lwp, "sky_stat.py"), "ref_lwp")
+    scan = _load("ref_lwp.sky_scan", os.path.join(lwp, "sky_scan.py"), "ref_lwp")
+    tdk = _load("ref_tdk", os.path.join(ref_root, "pycwb", "utils", "td_vector_kernels.py"))
+    return dpf, stat, scan, tdk
+
+
+# --------------------------------------------------------------------------
+# cases
+# --------------------------------------------------------------------------
+def _sky_case(name, ifos, healpix_order, n_pix, K, seed, snr=15.0, valid=None,
+              netCC=0.5, delta=0.5, gamma=0.5, acore=math.sqrt(2.0),
+              random_tables=False, n_sky=None, delta_regulator=None):
+    from pycwb_gb300.synthetic import make_cluster, regulators
+    from pycwb_gb300 import sky
+
+    rng = np.random.default_rng(seed)
+    n_ifo = len(ifos)
+    if random_tables:
+        n_sky = int(n_sky)
+        ml = rng.integers(-K, K + 1, size=(n_ifo, n_sky)).astype(np.int32)
+        ml[0] = 0
+        FP = rng.uniform(-1, 1, size=(n_ifo, n_sky))
+        FX = rng.uniform(-1, 1, size=(n_ifo, n_sky))
+    else:
+        ml, FP, FX = sky.compute_sky_delay_and_patterns(
+            ifos, ifos[0], 512.0, K, healpix_order=healpix_order)
+        n_sky = ml.shape[1]
+    FP_t = FP.T.astype(np.float32).copy()
+    FX_t = FX.T.astype(np.float32).copy()
+    td00, td90, rms, l_true = make_cluster(rng, ml, FP_t, FX_t, n_pix, K, snr)
+    reg = regulators(n_ifo, acore=acore, gamma=gamma, delta=delta, netCC=netCC)
+    if delta_regulator is not None:
+        # scan_sky_for_best_fit takes any delta_regulator; a negative one
+        # selects the likelihood-only sky statistic (sky_scan.py:141)
+        reg["delta_regulator"] = delta_regulator
+    if valid is None:
+        valid = np.arange(n_sky, dtype=np.int64)
+    return dict(name=name, n_ifo=n_ifo, n_pix=n_pix, n_sky=n_sky, FP=FP_t, FX=FX_t,
+                rms=rms, td00=td00, td90=td90, ml=ml, valid=np.asarray(valid, np.int64),
+                netCC=reg["netCC"], delta_regulator=reg["delta_regulator"],
+                gamma_regulator=reg["gamma_regulator"],
+                network_energy_threshold=reg["network_energy_threshold"],
+                l_true=l_true)
+
+
+def run_sky_case(ref, case):
+    dpf, _, scan, _ = ref
+    REG = np.array([case["delta_regulator"] * np.sqrt(2), 0.0, 0.0], dtype=np.float32)
+    REG[1] = dpf.calculate_dpf(case["FP"], case["FX"], case["rms"], case["n_sky"],
+                               case["n_ifo"], case["gamma_regulator"],
+                               case["network_energy_threshold"], case["valid"])
+    out = scan.scan_sky_for_best_fit(
+        case["n_ifo"], case["n_pix"], case["n_sky"], case["FP"], case["FX"], case["rms"],
+        case["td00"], case["td90"], case["ml"], REG, case["netCC"],
+        case["delta_regulator"], case["network_energy_threshold"], case["valid"])
+    res = dict(REG=REG, l_max=np.int64(out[0]), sky_stat_max=np.float64(out[12]),
+               stats=np.stack([np.asarray(a, np.float32) for a in out[1:12]]))
+    return res
+
+
+def _td_case(name, seed, M, n_coeffs, L, K, n_time, n_pix):
+    rng = np.random.default_rng(seed)
+    J = M * L
+    rows = n_time + 2 * n_coeffs
+    padded00 = np.zeros((rows, M + 1), np.float32)
+    padded90 = np.zeros((rows, M + 1), np.float32)
+    padded00[n_coeffs:n_coeffs + n_time] = rng.standard_normal((n_time, M + 1))
+    padded90[n_coeffs:n_coeffs + n_time] = rng.standard_normal((n_time, M + 1))
+    T0 = rng.standard_normal((2 * J + 1, 2 * n_coeffs + 1)) * 0.3
+    Tx = rng.standard_normal((2 * J + 1, 2 * n_coeffs + 1)) * 0.1
+    # keep every tap row in range: n_eff = n - wdm_shift stays in [0, n_time)
+    max_shift = (K + J - 1) // J
+    n = rng.integers(max_shift, n_time - max_shift, size=n_pix)
+    m = rng.integers(0, M + 1, size=n_pix)
+    m[:4] = [0, 1, M - 1, M]  # edge layers
+    idx = (n * (M + 1) + m).astype(np.int32)
+    return dict(name=name, pixel_indices=idx, padded00=padded00, padded90=padded90,
+                T0=T0, Tx=Tx, M=np.int64(M), n_coeffs=np.int64(n_coeffs),
+                K=np.int64(K), J=np.int64(J))
+
+
+def main(ref_root):
+    ref = load_reference(ref_root)
+    sky_cases = [
+        _sky_case("hlv_o2_p40", ["L1", "H1", "V1"], 2, 40, 20, seed=11),
+        _sky_case("hlv_o3_p24_subset", ["L1", "H1", "V1"], 3, 24, 20, seed=12,
+                  valid=np.sort(np.random.default_rng(5).choice(768, 300, replace=False))),
+        _sky_case("hlvk_o2_p30", ["L1", "H1", "V1", "K1"], 2, 30, 20, seed=13, snr=25.0),
+        _sky_case("hl_o2_p32", ["L1", "H1"], 2, 32, 20, seed=14),
+        _sky_case("hlv_o2_p40_deltaneg", ["L1", "H1", "V1"], 2, 40, 20, seed=15,
+                  delta_regulator=-0.3, netCC=0.0),
+        _sky_case("hlv_o2_p1", ["L1", "H1", "V1"], 2, 1, 20, seed=16, snr=8.0, netCC=0.0),
+        _sky_case("rand_s150_p50", ["L1", "H1", "V1"], None, 50, 20, seed=17,
+                  random_tables=True, n_sky=150, netCC=0.3),
+        _sky_case("hlv_o2_p40_netcc09", ["L1", "H1", "V1"], 2, 40, 20, seed=18, netCC=0.9),
+        _sky_case("hlv_o2_p20_k8", ["L1", "H1", "V1"], 2, 20, 8, seed=19),
+    ]
+    for case in sky_cases:
+        res = run_sky_case(ref, case)
+        path = os.path.join(HERE, f"sky_{case['name']}.npz")
+        np.savez_compressed(path, **{k: v for k, v in case.items() if k != "name"}, **res)
+        print(case["name"], "l_max", int(res["l_max"]), "stat", float(res["sky_stat_max"]),
+              "REG1", float(res["REG"][1]), "->", os.path.relpath(path, REPO))
+
+    tdk = ref[3]
+    td_cases = [
+        _td_case("m16_nc6_l1_k8", 21, M=16, n_coeffs=6, L=1, K=8, n_time=40, n_pix=64),
+        _td_case("m8_nc5_l1_k12", 22, M=8, n_coeffs=5, L=1, K=12, n_time=40, n_pix=48),
+        _td_case("m8_nc4_l2_k20", 23, M=8, n_coeffs=4, L=2, K=20, n_time=40, n_pix=48),
+        _td_case("m4_nc3_l1_k9", 24, M=4, n_coeffs=3, L=1, K=9, n_time=30, n_pix=32),
+    ]
+    for case in td_cases:
+        out = tdk.batch_get_td_vecs(case["pixel_indices"], case["padded00"], case["padded90"],
+                                    case["T0"], case["Tx"], int(case["M"]),
+                                    int(case["n_coeffs"]), int(case["K"]), int(case["J"]))
+        path = os.path.join(HERE, f"td_{case['name']}.npz")
+        np.savez_compressed(path, **{k: v for k, v in case.items() if k != "name"},
+                            out=np.asarray(out, np.float32))
+        print(case["name"], out.shape, "->", os.path.relpath(path, REPO))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYCWB_REFERENCE", ""))
