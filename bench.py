@@ -1,0 +1,482 @@
+#!/usr/bin/env python
+"""Benchmark of the batched coherent sky scan on GB300.
+
+Workload (one "step"): the batched sky loop of 4,096 synthetic clusters of
+one segment -- pixel counts log-uniform in [20, 3000], network SNR uniform
+in [8, 40], independent sky directions -- over the full HEALPix order-7 sky
+(196,608 directions) with L1/H1/V1 geometry, 41 delay samples (K = 20),
+float32 amplitudes.  One step = the DPF regulator and the sky scan of every
+cluster (pycwb/modules/likelihoodWP/likelihood.py:310-325 for each), as one
+persistent launch replayed from a CUDA graph.
+
+Reported (one JSON line on rank 0):
+  value       cluster-sky evaluations/s with inputs resident in HBM
+  e2e         the same through the public API (BatchedSkyLoop.run) with the
+              cluster data in pinned host memory: H2D of every step's inputs
+              and D2H of the per-cluster results inside the timed region
+  plain       the same kernel launched once per cluster on the same data
+  roofline    FP32 work of the sky-loop kernel against the measured FP32
+              FMA peak of the device
+  cpu_baseline  the CPU oracle (a restatement of the reference's loops,
+              OpenMP over the sky) on a bounded sample, all host cores
+
+--impl reference times the reference's CPU implementation (the oracle port;
+the reference's own compiled code needs numba/ROOT, absent here) on the
+same metric.  Under torchrun each rank evaluates its own 4,096 clusters
+(weak scaling; no collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "cluster-sky evals/s at HEALPix-7, 3 ifo: batched vs plain GPU at 1e-4 rel err"
+UNIT = "cluster-sky evals/s"
+IFOS = ("L1", "H1", "V1")
+K_TD = 20
+
+
+def ops_per_pair(n_ifo: int) -> int:
+    """Algorithmic FP32 ops per (direction, pixel): scan 77I+108 flops + 8 sqrt
+    + 12 div, regulator 23I+18 flops + 3 sqrt + 4 div (FMA = 2 flops,
+    sqrt/div = 1 op), counted from sky_stat.py:37-410, dpf.py:343-453 and
+    sky_scan.py:97-179."""
+    return (77 * n_ifo + 108 + 8 + 12) + (23 * n_ifo + 18 + 3 + 4)
+
+
+# --------------------------------------------------------------------------
+# helpers
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "power_w_median": float(np.median(power)) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value: float, device) -> float:
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sky_tables_np(order: int):
+    from pycwb_gb300 import sky
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(list(IFOS), IFOS[0], 512.0, K_TD,
+                                                    healpix_order=order)
+    return ml, FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (the oracle: the reference's loops restated in C, OpenMP)
+# --------------------------------------------------------------------------
+def cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=32, n_dirs=2048, seed=7, threads=0):
+    """Oracle regulator + scan of n_clusters size-stratified clusters, each on
+    n_dirs random directions.  Returns (seconds, pairs, evals)."""
+    from oracle import oracle
+    from pycwb_gb300.autotune import sample_indices
+
+    oracle.build()
+    rng = np.random.default_rng(seed)
+    n_sky = ml.shape[1]
+    idx = sample_indices(batch.sizes, n_clusters)
+    REG0 = np.float32(reg["delta_regulator"] * math.sqrt(2))
+    pairs = evals = 0
+    t0 = time.perf_counter()
+    for c in idx:
+        td00, td90, rms = batch.cluster_views(int(c))
+        valid = np.sort(rng.choice(n_sky, n_dirs, replace=False)).astype(np.int64)
+        reg1 = oracle.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
+                                    reg["network_energy_threshold"], valid, n_threads=threads)
+        REG = np.array([REG0, reg1, 0.0], np.float32)
+        oracle.scan_sky_for_best_fit(3, rms.shape[0], n_sky, FP_t, FX_t, rms, td00, td90, ml, REG,
+                                     reg["netCC"], reg["delta_regulator"],
+                                     reg["network_energy_threshold"], valid, n_threads=threads)
+        pairs += rms.shape[0] * n_dirs
+        evals += n_dirs
+    return time.perf_counter() - t0, pairs, evals, idx
+
+
+def cpu_rate(batch, ml, FP_t, FX_t, reg, target_s=12.0):
+    """Cluster-sky evals/s of the oracle on all host cores, normalised to the
+    workload's mean cluster size (evals/s = pairs/s / mean pixels)."""
+    cores = os.cpu_count() or 1
+    dt, pairs, _, _ = cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=8, n_dirs=256)
+    rate = pairs / dt
+    n_dirs = int(min(ml.shape[1], max(256, target_s * rate / (32 * float(batch.sizes.mean())))))
+    dt, pairs, evals, idx = cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=32, n_dirs=n_dirs)
+    pair_rate = pairs / dt
+    value = pair_rate / float(batch.sizes.mean())
+    sample = (f"oracle float32 (regulator + scan) on {len(idx)} size-stratified clusters of the "
+              f"workload x {n_dirs} random directions each, {pairs:.3e} direction-pixel pairs in "
+              f"{dt:.1f} s; evals/s = pairs/s / mean cluster size {batch.sizes.mean():.1f}")
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "seconds": dt}
+
+
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--clusters", type=int, default=4096)
+    ap.add_argument("--order", type=int, default=7)
+    ap.add_argument("--seed", type=int, default=20240914)
+    ap.add_argument("--fast-math", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shape")
+    ap.add_argument("--profile", action="store_true",
+                    help="one eager launch of the batched loop and exit (for ncu)")
+    args = ap.parse_args()
+
+    world, rank, local, pg = dist_setup()
+    from pycwb_gb300.synthetic import log_uniform_sizes, regulators
+
+    reg = regulators(len(IFOS))
+    n_sky_expected = 12 * 4 ** args.order
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ml, FP_t, FX_t = sky_tables_np(args.order)
+        rng = np.random.default_rng(args.seed)
+        sizes = log_uniform_sizes(rng, args.clusters, 20, 3000)
+        from pycwb_gb300.likelihoodWP.batched import ClusterBatch
+        from pycwb_gb300.synthetic import make_cluster
+        # the reference arm needs host data of only the sampled clusters
+        from pycwb_gb300.autotune import sample_indices
+        keep = set(int(c) for c in sample_indices(sizes, 32))
+        batch = ClusterBatch.__new__(ClusterBatch)
+        batch.sizes = sizes
+        views = {}
+        for c in sorted(keep):
+            td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, int(sizes[c]), K_TD,
+                                              float(rng.uniform(8, 40)))
+            views[c] = (td00, td90, rms)
+        batch.cluster_views = lambda c: views[int(c)]
+        cores = os.cpu_count() or 1
+        vals = []
+        for step in range(args.warmup + args.steps):
+            dt, pairs, evals, idx = cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=32,
+                                               n_dirs=256, seed=step)
+            if step >= args.warmup:
+                vals.append(pairs / dt / float(sizes.mean()))
+        v = float(np.median(vals))
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+                "config": {"workload": "batched sky loop, 4096 clusters P~logU[20,3000], "
+                                       f"HEALPix {args.order}, 3 ifo, 41 delays", "clusters": args.clusters},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": "oracle float32 (a restatement of the reference's "
+                                           "dpf.py/sky_stat.py/sky_scan.py loops; the reference's "
+                                           "own numba code cannot be installed offline) on 32 "
+                                           "size-stratified clusters x 256 random directions per "
+                                           "step, normalised by the workload's mean cluster size"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    from pycwb_gb300 import _lib
+    from pycwb_gb300.autotune import autotune
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch, SkyTables
+    from pycwb_gb300.synthetic import make_batch_device
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.build()
+    L = _lib.load()
+
+    ml, FP_t, FX_t = sky_tables_np(args.order)
+    n_sky = ml.shape[1]
+    assert n_sky == n_sky_expected
+    tables = SkyTables.from_arrays(FP_t, FX_t, ml, None, **{k: reg[k] for k in (
+        "network_energy_threshold", "gamma_regulator", "delta_regulator", "netCC")})
+
+    rng = np.random.default_rng(args.seed + 1000 * rank)
+    sizes = log_uniform_sizes(rng, args.clusters, 20, 3000)
+    batch = ClusterBatch(len(IFOS), 2 * K_TD + 1, sizes)
+    t_gen = time.perf_counter()
+    td00, td90, rms, l_true, snr = make_batch_device(args.seed + 1000 * rank, sizes, ml, FP_t,
+                                                     FX_t, K_TD, device=dev)
+    batch.td00.copy_(td00)
+    batch.td90.copy_(td90)
+    batch.rms.copy_(rms)
+    del td00, td90, rms
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
+
+    shape = None if args.no_tune else autotune(tables, batch, fast_math=bool(args.fast_math))
+    if shape is None:
+        shape = _lib.TileShape(0, 0, 0, 0, 0, int(args.fast_math))
+    loop = BatchedSkyLoop(tables, batch, shape=shape)
+    loop.upload()
+    loop.stream.synchronize()
+
+    if args.profile:
+        loop.launch()
+        loop.stream.synchronize()
+        print(json.dumps({"profile": "one launch", "clusters": args.clusters}))
+        return
+
+    total_pix = batch.total_pix
+    n_valid = n_sky
+    work_evals = args.clusters * n_valid            # cluster-sky evaluations per step
+    work_pairs = total_pix * n_valid
+    ops = ops_per_pair(len(IFOS)) * work_pairs
+
+    # ---- device-resident timed region ------------------------------------
+    loop.capture()
+    for _ in range(args.warmup):
+        loop.replay()
+    loop.stream.synchronize()
+    barrier(pg)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(loop.stream)
+    for k in range(args.steps):
+        loop.replay()
+        evs[k + 1].record(loop.stream)
+    loop.stream.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(pg)
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    total_ms = max_over_ranks(pg, total_ms, dev)
+    ms_per_step = total_ms / args.steps
+    value = world * work_evals / (ms_per_step * 1e-3)
+    loop.download()
+    loop.stream.synchronize()
+    res = loop.results()
+
+    # ---- FP32 roofline ---------------------------------------------------
+    peak = ctypes_peak(L)
+    kernel_ms = float(np.median(step_ms))
+    achieved = ops / (kernel_ms * 1e-3) / 1e12
+    traffic = traffic_from_profile(total_pix, n_valid)
+
+    # ---- plain: one launch per cluster on the same device data ------------
+    plain = None
+    if not args.no_plain:
+        plain = time_plain(L, loop, tables, batch, shape, dev)
+        plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
+
+    # ---- end to end through the public API ------------------------------
+    e2e = None
+    if not args.no_e2e:
+        loop.run()  # warm
+        barrier(pg)
+        t0 = time.perf_counter()
+        n_e2e = max(1, min(args.steps, 2))
+        for _ in range(n_e2e):
+            loop.run(upload=True, download=True)
+        dt = (time.perf_counter() - t0) / n_e2e
+        dt = max_over_ranks(pg, dt, dev)
+        e2e = {"value": world * work_evals / dt, "unit": UNIT,
+               "h2d_bytes_per_step": batch.h2d_bytes, "d2h_bytes_per_step": loop.d2h_bytes,
+               "ms_per_step": dt * 1e3, "steps": n_e2e, "api": "BatchedSkyLoop.run"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_rate(batch, ml, FP_t, FX_t, reg)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {
+                "workload": (f"batched sky loop (regulator + scan), {args.clusters} clusters, "
+                             f"pixels log-uniform[20,3000], SNR U[8,40], HEALPix {args.order} "
+                             f"({n_sky} directions), L1/H1/V1, 41 delays, float32"),
+                "clusters": args.clusters, "total_pix": total_pix, "n_sky": n_sky,
+                "healpix_order": args.order, "n_ifo": 3, "n_delay": 2 * K_TD + 1,
+                "launch_shape": dict(zip(("threads", "lanes_per_sky", "chunk_pix", "stages",
+                                          "min_blocks", "fast_math"), shape.key())),
+                "l2": "inputs larger than L2: 2.4 GB td amplitudes + 35 GB maps per step",
+                "generation_s": round(t_gen, 2),
+            },
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "ops_per_launch": ops, "ops_per_pair": ops_per_pair(3),
+                         "kernel_ms": kernel_ms,
+                         "peak_source": "measured: pgw_fp32_fma_peak (register FMA chains, "
+                                        "2 flops per FMA) in this run"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 3 * args.steps,
+            "clocks": clk,
+            "plain": plain,
+            "batched_vs_plain": (plain["ms"] / ms_per_step) if plain else None,
+            "selected": {"found": int(res.found.sum()),
+                         "l_max_equals_injected": int(np.sum(res.l_max == l_true))},
+            "step_ms": step_ms,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def ctypes_peak(L):
+    import ctypes
+    import torch
+    out = ctypes.c_double(0.0)
+    ms = ctypes.c_double(0.0)
+    rc = L.pgw_fp32_fma_peak(20000, ctypes.byref(out), ctypes.byref(ms),
+                             torch.cuda.current_stream().cuda_stream)
+    return out.value if rc == 0 else None
+
+
+def traffic_from_profile(total_pix, n_valid):
+    """DRAM bytes per launch scaled from the committed ncu summary, or None."""
+    path = os.path.join(REPO, "profiles", "sky_loop_traffic.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["dram_bytes_per_pair"]) * total_pix * n_valid + float(
+            p.get("dram_bytes_per_direction_cluster", 0.0)) * n_valid
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def time_plain(L, loop, tables, batch, shape, dev):
+    """The same clusters, one pgw_sky_loop launch each (device-resident)."""
+    import ctypes
+    import torch
+
+    n_sky = tables.n_sky
+    s = loop.stream
+    with torch.cuda.stream(s):
+        ws = torch.empty(L.pgw_workspace_bytes(batch.n_ifo, batch.n_delay, int(batch.sizes.max()), 1),
+                         dtype=torch.uint8, device=dev)
+        st = torch.empty((11, n_sky), dtype=torch.float32, device=dev)
+        res = torch.empty((batch.n_clusters, 24), dtype=torch.uint8, device=dev)
+        regs = torch.empty(batch.n_clusters, dtype=torch.float64, device=dev)
+    ptrs = []
+    for c in range(batch.n_clusters):
+        a, b = int(batch.td_offsets[c]), int(batch.pix_offsets[c])
+        ptrs.append((int(batch.sizes[c]), loop.td00.data_ptr() + 4 * a, loop.td90.data_ptr() + 4 * a,
+                     loop.rms.data_ptr() + 4 * batch.n_ifo * b))
+    shp = ctypes.byref(shape) if shape is not None else None
+
+    def one(c):
+        P, t0, t9, rm = ptrs[c]
+        rc = L.pgw_sky_loop(batch.n_ifo, P, n_sky, tables.FP.data_ptr(), tables.FX.data_ptr(), rm,
+                            t0, t9, batch.n_delay, tables.ml.data_ptr(), tables.REG0,
+                            tables.gamma_regulator, tables.netCC, tables.network_energy_threshold,
+                            tables.valid.data_ptr(), tables.valid.numel(), st.data_ptr(),
+                            res.data_ptr() + 24 * c, regs.data_ptr() + 8 * c, shp, ws.data_ptr(),
+                            ws.numel(), s.cuda_stream)
+        if rc:
+            raise RuntimeError(L.pgw_last_error().decode())
+
+    for c in range(min(64, batch.n_clusters)):  # warm-up
+        one(c)
+    s.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for c in range(batch.n_clusters):
+        one(c)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"ms": ms, "launches": batch.n_clusters * 3,
+            "note": "same kernel, one pgw_sky_loop per cluster, device-resident, 1 timed pass"}
+
+
+if __name__ == "__main__":
+    main()

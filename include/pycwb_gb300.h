@@ -1,0 +1,168 @@
+/*
+ * pycwb_gb300 — C ABI of the GB300 (sm_103a) coherent sky-scan likelihood.
+ *
+ * Plain C types only: every array is a DEVICE pointer (CUDA global memory),
+ * every size is an integer, `stream` is a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  Calls are asynchronous on `stream` and
+ * allocate nothing: scratch memory is the caller's `workspace` (size from
+ * pgw_workspace_bytes).  Host-side argument errors return a pgw_status at
+ * once; errors found by a kernel (a delay index outside the td window, an
+ * expired wait) are written as bits (1 << code) into the `status` field of
+ * the pgw_scan_result the call fills, which the caller reads back together
+ * with l_max.  No call aborts, traps or waits without a time limit.
+ *
+ * Array layouts are the reference's (pycwb/modules/likelihoodWP):
+ *   FP, FX   (n_sky, n_ifo) float32   likelihood_setup.py:162-163
+ *   ml       (n_ifo, n_sky) int32     detector.py:1318-1321
+ *   rms      (n_pix, n_ifo) float32   likelihood.py:305
+ *   td00/90  (n_delay, n_ifo, n_pix) float32, n_delay = 2K+1
+ *                                     likelihood.py:303-304
+ *   stats    (11, n_sky) float32 in the order of the reference's return
+ *            tuple (sky_scan.py:191-192): antenna prior, alignment,
+ *            likelihood, null energy, coherent energy, correlation, sky
+ *            statistic, disbalance, network index, ellipticity, polarisation.
+ */
+#ifndef PYCWB_GB300_H
+#define PYCWB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGW_MAX_IFO 8
+#define PGW_N_STATS 11
+
+typedef enum {
+  PGW_OK = 0,
+  PGW_ERR_BAD_SHAPE = 1,       /* shape/size argument out of range (reference: ValueError, dpf.py:14-22) */
+  PGW_ERR_BAD_ARGUMENT = 2,    /* NULL pointer or misaligned buffer */
+  PGW_ERR_CUDA = 3,            /* a CUDA runtime call failed; see pgw_last_error() */
+  PGW_ERR_WORKSPACE = 4,       /* workspace smaller than pgw_workspace_bytes() */
+  PGW_ERR_DELAY_RANGE = 5,     /* device: ml[i,l] + K outside [0, n_delay) */
+  PGW_ERR_TIMEOUT = 6,         /* device: a bounded wait expired */
+  PGW_ERR_SKY_INDEX = 7        /* device: a sky_valid_indices entry outside [0, n_sky) */
+} pgw_status;
+
+/* Result of one cluster's sky scan, written by the device. */
+typedef struct {
+  int64_t l_max;        /* selected sky index (sky_scan.py:183-189: >=, last tie wins) */
+  float sky_stat_max;   /* statistic at l_max; 0 when no direction qualified */
+  int32_t found;        /* 0: no valid direction reached the >= comparison; l_max = valid[0] */
+  int32_t status;       /* OR of (1 << pgw_status) for device-detected errors */
+  float regulator;      /* REG[1] used by the scan (float32, as stored by likelihood.py:310) */
+} pgw_scan_result;
+
+/* Library version string. */
+const char* pgw_version(void);
+
+/* Message of the last failing call on this host thread ("" when none). */
+const char* pgw_last_error(void);
+
+/* Bytes of scratch a call needs for n_clusters clusters holding total_pix
+ * pixels in all (plain calls: n_clusters = 1, total_pix = n_pix). */
+size_t pgw_workspace_bytes(int n_ifo, int n_delay, int64_t total_pix, int n_clusters);
+
+/* DPF regulator: REG[1] = (n_valid^2 / (n_pass^2 + 1e-9) - 1) * E_thr, where
+ * n_pass counts valid directions whose DPF quality sqrt(NI / (NN + 0.01))
+ * exceeds gamma_regulator.
+ * Replaces calculate_dpf, pycwb/modules/likelihoodWP/dpf.py:7-34.
+ * Writes *out_regulator (float64, device) and, when REG != NULL, REG[1]
+ * (float32, device) so the scan can consume it without a host round trip. */
+int pgw_calculate_dpf(const float* FP, const float* FX, const float* rms, int64_t n_sky,
+                      int n_ifo, int64_t n_pix, double gamma_regulator,
+                      double network_energy_threshold, const int64_t* sky_valid_indices,
+                      int64_t n_valid, double* out_regulator, float* REG, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Sky scan over the valid directions with a given REG (device, 3 floats).
+ * Replaces scan_sky_for_best_fit, pycwb/modules/likelihoodWP/sky_scan.py:17-192.
+ * out_stats: (11, n_sky) float32; entries of directions that are masked or
+ * rejected are 0, as in the reference. */
+int pgw_scan_sky_for_best_fit(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP,
+                              const float* FX, const float* rms, const float* td00,
+                              const float* td90, int n_delay, const int32_t* ml, const float* REG,
+                              double netCC, double delta_regulator,
+                              double network_energy_threshold,
+                              const int64_t* sky_valid_indices, int64_t n_valid, float* out_stats,
+                              pgw_scan_result* out_result, void* workspace, size_t workspace_bytes,
+                              void* stream);
+
+/* Launch shape of the sky-loop kernel (any field 0 = automatic).
+ *   threads        CTA size, a multiple of 32 in [64, 256]
+ *   lanes_per_sky  1, 2 or 4 lanes share one direction and split its pixels
+ *   chunk_pix      pixels per chunk staged in shared memory by one TMA copy
+ *   stages         chunks in flight per CTA, 2..4
+ *   min_blocks     occupancy target the kernel is compiled for: 3 or 4 CTAs
+ *                  per SM for n_ifo <= 4, 2 above
+ *   fast_math      1: the scan divides with div.full.f32 (2 ulp) and takes
+ *                  square roots with sqrt.approx.f32; 0: IEEE div/sqrt.
+ *                  The regulator pass always uses IEEE arithmetic. */
+typedef struct {
+  int threads;
+  int lanes_per_sky;
+  int chunk_pix;
+  int stages;
+  int min_blocks;
+  int fast_math;
+} pgw_tile_shape;
+
+/* Both passes for one cluster in one launch: the regulator, then the scan
+ * with REG = {REG0, regulator, 0}.  Replaces the two calls at
+ * pycwb/modules/likelihoodWP/likelihood.py:310-325 ("plain" path).  shape
+ * may be NULL. */
+int pgw_sky_loop(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP, const float* FX,
+                 const float* rms, const float* td00, const float* td90, int n_delay,
+                 const int32_t* ml, float REG0, double gamma_regulator, double netCC,
+                 double network_energy_threshold, const int64_t* sky_valid_indices,
+                 int64_t n_valid, float* out_stats, pgw_scan_result* out_result,
+                 double* out_regulator, const pgw_tile_shape* shape, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* Regulator and scan for many clusters of one segment in ONE persistent
+ * launch driven by a work queue of (cluster, sky tile) items taken in
+ * decreasing cluster size.  Replaces the per-cluster loop of
+ * evaluate_fragment_clusters, pycwb/modules/likelihoodWP/likelihood.py:58-135
+ * (its calls at :310-325).  shape may be NULL.  Clusters are concatenated along the pixel axis:
+ * cluster c owns pixels [pix_offsets[c], pix_offsets[c+1]) of rms_all
+ * (total_pix, n_ifo) and the float32 block of n_delay*n_ifo*n_pix_c values
+ * starting at td_offsets[c] in td00_all/td90_all, laid out (n_delay, n_ifo,
+ * n_pix_c) like the plain call.  pix_offsets and td_offsets are device int64
+ * arrays of n_clusters+1 entries; total_pix = pix_offsets[n_clusters] (given
+ * on the host to size the workspace).  out_stats: (n_clusters, 11, n_sky);
+ * out_results and out_regulators: n_clusters entries. */
+int pgw_sky_loop_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
+                         const int64_t* td_offsets, int64_t total_pix, int64_t n_sky, const float* FP, const float* FX, const float* rms_all,
+                         const float* td00_all, const float* td90_all, int n_delay,
+                         const int32_t* ml, float REG0, double gamma_regulator, double netCC,
+                         double network_energy_threshold, const int64_t* sky_valid_indices,
+                         int64_t n_valid, float* out_stats, pgw_scan_result* out_results,
+                         double* out_regulators, const pgw_tile_shape* shape, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* td-amplitude vectors of n_pixels pixels of one (layer, detector) plane:
+ * out (n_pixels, 4K+2) float32 = [a00(-K..K), a90(-K..K)] per pixel.
+ * Replaces batch_get_td_vecs, pycwb/utils/td_vector_kernels.py:133-199
+ * (getTDamp, cwb-core/WDM.cc:1103-1196).  padded00/90: (rows, M+1) float32
+ * planes padded by n_coeffs zero rows at both ends; T0, Tx: (2J+1,
+ * 2*n_coeffs+1) float64 TD filters; phase: (M+1, 2J+1, 4) float64 factors
+ * {cos(same), sin(same), sin(low), sin(high)} (see pycwb_gb300.tdamp).
+ * Bit-identical to the reference: float64 accumulation in its order. */
+int pgw_batch_get_td_vecs(const int32_t* pixel_indices, int64_t n_pixels, const float* padded00,
+                          const float* padded90, int64_t rows, const double* T0, const double* Tx,
+                          const double* phase, int M, int n_coeffs, int K, int J, float* out,
+                          void* stream);
+
+/* Diagnostics (no counterpart in the reference).  Measures the device's
+ * FP32 fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) with one
+ * timed launch of `iters` x 128 register FMAs per thread; the sky loop's
+ * FP32 roofline is reported against this number.  Synchronous. */
+int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYCWB_GB300_H */

@@ -43,9 +43,9 @@ def lib():
         L.oracle_calculate_dpf_f32.argtypes = [P, P, P, i64, i32, i64, f64, f64, P, i64, i32, P]
         L.oracle_calculate_dpf_f64.argtypes = [P, P, P, i64, i32, i64, f64, f64, P, i64, i32, P]
         L.oracle_scan_sky_f32.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, P, f64, f64, f64,
-                                          P, i64, i32, P, P, P, P]
+                                          P, i64, i32, P, P, P, P, P]
         L.oracle_scan_sky_f64.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, P, f64, f64,
-                                          P, i64, i32, P, P, P]
+                                          P, i64, i32, P, P, P, P]
         L.oracle_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, i32, i32, i32, i32, P,
                                                i32, P]
         for f in (L.oracle_calculate_dpf_f32, L.oracle_calculate_dpf_f64, L.oracle_scan_sky_f32,
@@ -79,8 +79,12 @@ def calculate_dpf(FP, FX, rms, n_sky, n_ifo, gamma_regulator, network_energy_thr
 
 def scan_sky_for_best_fit(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG, netCC,
                           delta_regulator, network_energy_threshold, sky_valid_indices,
-                          n_threads=0, precision="f32"):
-    """Returns the reference's 13-tuple (sky_scan.py:191-192)."""
+                          n_threads=0, precision="f32", return_ellipticity=False):
+    """Returns the reference's 13-tuple (sky_scan.py:191-192).
+
+    return_ellipticity=True appends an (n_sky,) array holding
+    the ellipticity Cr of every valid direction, also those that the netCC
+    cut rejects (NaN elsewhere) -- used to recognise near-threshold cuts."""
     FP, FX, rms = _c(FP, np.float32), _c(FX, np.float32), _c(rms, np.float32)
     td00, td90 = _c(td00, np.float32), _c(td90, np.float32)
     ml = _c(ml, np.int32)
@@ -91,21 +95,28 @@ def scan_sky_for_best_fit(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG,
         REGa = _c(REG, np.float32)
         stats = np.zeros((N_STATS, int(n_sky)), np.float32)
         found = np.zeros(1, np.int32)
+        cr = np.full(int(n_sky), np.nan, np.float32)
         rc = lib().oracle_scan_sky_f32(int(n_ifo), int(n_pix), int(n_sky), _p(FP), _p(FX), _p(rms),
                                        _p(td00), _p(td90), td00.shape[0], _p(ml), _p(REGa),
                                        float(netCC), float(delta_regulator),
                                        float(network_energy_threshold), _p(valid), valid.size,
-                                       int(n_threads), _p(stats), _p(l_max), _p(smax), _p(found))
+                                       int(n_threads), _p(stats), _p(l_max), _p(smax), _p(found),
+                                       _p(cr))
     else:
         REGa = _c(REG, np.float64)
         stats = np.zeros((N_STATS, int(n_sky)), np.float64)
+        cr = np.full(int(n_sky), np.nan, np.float64)
         rc = lib().oracle_scan_sky_f64(int(n_ifo), int(n_pix), int(n_sky), _p(FP), _p(FX), _p(rms),
                                        _p(td00), _p(td90), td00.shape[0], _p(ml), _p(REGa),
                                        float(netCC), float(network_energy_threshold), _p(valid),
-                                       valid.size, int(n_threads), _p(stats), _p(l_max), _p(smax))
+                                       valid.size, int(n_threads), _p(stats), _p(l_max), _p(smax),
+                                       _p(cr))
     if rc:
         raise ValueError(f"oracle scan_sky_for_best_fit failed ({rc})")
-    return (int(l_max[0]),) + tuple(stats[k] for k in range(N_STATS)) + (float(smax[0]),)
+    out = (int(l_max[0]),) + tuple(stats[k] for k in range(N_STATS)) + (float(smax[0]),)
+    if return_ellipticity:
+        out = out + (cr,)
+    return out
 
 
 def batch_get_td_vecs(pixel_indices, padded00, padded90, T0, Tx, M, n_coeffs, K, J,

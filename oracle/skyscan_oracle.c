@@ -131,7 +131,7 @@ static inline int scan_sky32(int I, int64_t P, int64_t l, const float* FP, const
                              const float* rms, const float* td00, const float* td90,
                              int n_delay, int64_t n_sky, const int32_t* ml, float rr, float RR,
                              double netCC, double delta_regulator, float ethr32,
-                             float* stats /* N_STATS x n_sky */, float* best) {
+                             float* stats /* N_STATS x n_sky */, float* best, float* cr_all) {
   const int off = n_delay / 2;                           /* sky_scan.py:92 */
   int row[ORC_MAXIFO];
   for (int i = 0; i < I; ++i) {
@@ -255,6 +255,7 @@ static inline int scan_sky32(int I, int64_t P, int64_t l, const float* FP, const
     ccor = 1.0;   /* Python float 1.0: null*1.0 stays float32 and (Ec+No) rounds to float32 */
     corr = (double)EC / ((double)(EC + No) - (double)(Mo * (I - 1)));
   }
+  if (cr_all) cr_all[l] = Cr;  /* ellipticity of every valid direction (diagnostic) */
   if (!isfinite(Cr) || (double)Cr < netCC) return ORC_OK;  /* :135-136 */
 
   float Lk = Eo > 0.0f ? Eo - No : 0.0f;                 /* :139 */
@@ -298,7 +299,7 @@ int oracle_scan_sky_f32(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP
                         const int32_t* ml, const float* REG, double netCC, double delta_regulator,
                         double network_energy_threshold, const int64_t* valid, int64_t n_valid,
                         int n_threads, float* stats, int64_t* l_max, double* sky_stat_max,
-                        int* found) {
+                        int* found, float* cr_all) {
   if (n_ifo < 1 || n_ifo > ORC_MAXIFO || n_pix < 0 || n_sky < 1 || n_valid < 1 || n_delay < 1)
     return ORC_BAD_SHAPE;
   set_threads(n_threads);
@@ -312,7 +313,7 @@ int oracle_scan_sky_f32(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP
 #pragma omp parallel for schedule(dynamic, 16)
   for (int64_t k = 0; k < n_valid; ++k) {
     int e = scan_sky32(n_ifo, n_pix, valid[k], FP, FX, rms, td00, td90, n_delay, n_sky, ml, rr,
-                       RR, netCC, delta_regulator, ethr32, stats, best);
+                       RR, netCC, delta_regulator, ethr32, stats, best, cr_all);
     if (e) {
 #pragma omp atomic write
       err = e;
@@ -391,7 +392,8 @@ int oracle_calculate_dpf_f64(const float* FP, const float* FX, const float* rms,
 static inline int scan_sky64(int I, int64_t P, int64_t l, const float* FP, const float* FX,
                              const float* rms, const float* td00, const float* td90,
                              int n_delay, int64_t n_sky, const int32_t* ml, double rr, double RR,
-                             double netCC, double ethr, double* stats, double* best) {
+                             double netCC, double ethr, double* stats, double* best,
+                             double* cr_all) {
   const int off = n_delay / 2;
   int row[ORC_MAXIFO];
   for (int i = 0; i < I; ++i) {
@@ -465,6 +467,7 @@ static inline int scan_sky64(int I, int64_t P, int64_t l, const float* FP, const
   double CH = No / ((double)(I * Mo) + sqrt((double)Mo));
   double ccor = CH > 1.0 ? CH : 1.0;
   double corr = EC / (EC + No * ccor - (double)(Mo * (I - 1)));
+  if (cr_all) cr_all[l] = Cr;
   if (!isfinite(Cr) || Cr < netCC) return ORC_OK;
   double Lk = Eo > 0 ? Eo - No : 0.0;
   double AA = Lk * corr;
@@ -489,7 +492,8 @@ int oracle_scan_sky_f64(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP
                         const float* rms, const float* td00, const float* td90, int n_delay,
                         const int32_t* ml, const double* REG, double netCC,
                         double network_energy_threshold, const int64_t* valid, int64_t n_valid,
-                        int n_threads, double* stats, int64_t* l_max, double* sky_stat_max) {
+                        int n_threads, double* stats, int64_t* l_max, double* sky_stat_max,
+                        double* cr_all) {
   if (n_ifo < 1 || n_ifo > ORC_MAXIFO || n_pix < 0 || n_sky < 1 || n_valid < 1 || n_delay < 1)
     return ORC_BAD_SHAPE;
   set_threads(n_threads);
@@ -501,7 +505,7 @@ int oracle_scan_sky_f64(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP
 #pragma omp parallel for schedule(dynamic, 16)
   for (int64_t k = 0; k < n_valid; ++k) {
     int e = scan_sky64(n_ifo, n_pix, valid[k], FP, FX, rms, td00, td90, n_delay, n_sky, ml,
-                       REG[0], REG[1], netCC, network_energy_threshold, stats, best);
+                       REG[0], REG[1], netCC, network_energy_threshold, stats, best, cr_all);
     if (e) {
 #pragma omp atomic write
       err = e;

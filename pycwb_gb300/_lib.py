@@ -1,0 +1,142 @@
+"""Build and load the native library (libpycwb_gb300.so, CUDA sm_103a).
+
+The library exports the C ABI declared in include/pycwb_gb300.h.  It is
+built in-tree with nvcc; Python reaches it through ctypes and passes raw
+device pointers and CUDA stream handles taken from torch tensors (torch is
+used for device memory and streams only).  There is no fallback: if the
+library is missing or CUDA is unavailable, the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(REPO, "include")
+LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
+SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu"]
+HEADERS = ["common.cuh"]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+_lock = threading.Lock()
+_lib = None
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
+    deps.append(os.path.join(INCLUDE, "pycwb_gb300.h"))
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every translation unit in parallel and link the shared library."""
+    with _lock:
+        if not force and not _stale():
+            return LIB_PATH
+        objs, procs = [], []
+        for src in SOURCES:
+            obj = os.path.join(CSRC, src.replace(".cu", ".o"))
+            cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+            if verbose:
+                cmd.insert(1, "-Xptxas=-v")
+            procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE,
+                                                stderr=subprocess.STDOUT, text=True)))
+            objs.append(obj)
+        errors = []
+        for src, p in procs:
+            out, _ = p.communicate()
+            if verbose and out:
+                print(out)
+            if p.returncode != 0:
+                errors.append(f"{src}:\n{out}")
+        if errors:
+            raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+        tmp = LIB_PATH + ".tmp"
+        subprocess.run([nvcc(), ARCH, "-shared", "-o", tmp] + objs + ["-lcudart"], check=True)
+        os.replace(tmp, LIB_PATH)
+        return LIB_PATH
+
+
+def load():
+    """The loaded library with argument types set (raises if it cannot load)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: run pycwb_gb300._lib.build() (needs nvcc)")
+        L = ctypes.CDLL(LIB_PATH)
+        P, i32, i64, f32, f64, sz = (ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                     ctypes.c_float, ctypes.c_double, ctypes.c_size_t)
+        L.pgw_version.restype = ctypes.c_char_p
+        L.pgw_last_error.restype = ctypes.c_char_p
+        L.pgw_workspace_bytes.argtypes = [i32, i32, i64, i32]
+        L.pgw_workspace_bytes.restype = sz
+        L.pgw_calculate_dpf.argtypes = [P, P, P, i64, i32, i64, f64, f64, P, i64, P, P, P, sz, P]
+        L.pgw_scan_sky_for_best_fit.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, P, f64, f64,
+                                                f64, P, i64, P, P, P, sz, P]
+        L.pgw_sky_loop.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64, f64, P,
+                                   i64, P, P, P, P, P, sz, P]
+        L.pgw_sky_loop_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
+                                           f64, f64, f64, P, i64, P, P, P, P, P, sz, P]
+        L.pgw_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, P, i32, i32, i32, i32, P, P]
+        L.pgw_fp32_fma_peak.argtypes = [i32, P, P, P]
+        for name in ("pgw_fp32_fma_peak", "pgw_calculate_dpf", "pgw_scan_sky_for_best_fit", "pgw_sky_loop",
+                     "pgw_sky_loop_batched", "pgw_batch_get_td_vecs"):
+            getattr(L, name).restype = ctypes.c_int
+        _lib = L
+        return _lib
+
+
+class TileShape(ctypes.Structure):
+    """pgw_tile_shape (include/pycwb_gb300.h); 0 in a field = automatic."""
+    _fields_ = [("threads", ctypes.c_int), ("lanes_per_sky", ctypes.c_int),
+                ("chunk_pix", ctypes.c_int), ("stages", ctypes.c_int),
+                ("min_blocks", ctypes.c_int), ("fast_math", ctypes.c_int)]
+
+    def key(self):
+        return (self.threads, self.lanes_per_sky, self.chunk_pix, self.stages, self.min_blocks,
+                self.fast_math)
+
+
+STATUS_NAMES = {
+    1: "bad shape", 2: "bad argument", 3: "CUDA error", 4: "workspace too small",
+    5: "delay index outside the td window", 6: "bounded wait expired",
+    7: "sky index outside [0, n_sky)",
+}
+
+
+def check(rc: int, what: str) -> None:
+    """Turn a pgw_status into the reference's exception types."""
+    if rc == 0:
+        return
+    msg = load().pgw_last_error().decode(errors="replace")
+    if rc in (1, 2, 4):
+        raise ValueError(f"{what}: {STATUS_NAMES.get(rc, rc)}: {msg}")
+    raise RuntimeError(f"{what}: {STATUS_NAMES.get(rc, rc)}: {msg}")
+
+
+def check_device_status(status: int, what: str) -> None:
+    if status == 0:
+        return
+    names = [STATUS_NAMES.get(b, str(b)) for b in range(32) if status & (1 << b)]
+    raise RuntimeError(f"{what}: device reported " + ", ".join(names))

@@ -1,0 +1,254 @@
+"""Batched sky loop: thousands of clusters of one segment in one launch.
+
+Replaces the per-cluster loop of evaluate_fragment_clusters
+(pycwb/modules/likelihoodWP/likelihood.py:58-135) around its two sky-loop
+calls (:310-325).  Per-segment tables (F+, Fx, delay indices, sky mask) are
+uploaded once (SkyTables, the device side of prepare_likelihood_inputs,
+likelihood_setup.py:81-238); the clusters of a lag are concatenated along
+the pixel axis (ClusterBatch); one persistent kernel launch evaluates the
+regulator and the scan of every cluster, taking (cluster, sky tile) work
+items in decreasing cluster size.  The launch can be captured in a CUDA
+graph and replayed.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .. import _device as dv
+from .. import _lib
+from .sky_scan import N_STATS
+
+
+@dataclass
+class SkyTables:
+    """Per-segment sky tables resident on the device.
+
+    FP, FX (n_sky, n_ifo) float32, ml (n_ifo, n_sky) int32, valid (n_valid,)
+    int64, plus the segment constants of likelihood_setup.py:140-147.
+    """
+
+    FP: torch.Tensor
+    FX: torch.Tensor
+    ml: torch.Tensor
+    valid: torch.Tensor
+    n_ifo: int
+    n_sky: int
+    network_energy_threshold: float
+    gamma_regulator: float
+    delta_regulator: float
+    netCC: float
+
+    @classmethod
+    def from_arrays(cls, FP_t, FX_t, ml, sky_valid_indices=None, *, network_energy_threshold,
+                    gamma_regulator, delta_regulator, netCC):
+        n_sky, n_ifo = dv.shape_of(FP_t)
+        if dv.shape_of(FX_t) != (n_sky, n_ifo) or dv.shape_of(ml) != (n_ifo, n_sky):
+            raise ValueError("FP/FX must be (n_sky, n_ifo) and ml (n_ifo, n_sky)")
+        if sky_valid_indices is None:
+            sky_valid_indices = np.arange(n_sky, dtype=np.int64)
+        return cls(FP=dv.to_device(FP_t, torch.float32), FX=dv.to_device(FX_t, torch.float32),
+                   ml=dv.to_device(ml, torch.int32),
+                   valid=dv.to_device(sky_valid_indices, torch.int64), n_ifo=int(n_ifo),
+                   n_sky=int(n_sky), network_energy_threshold=float(network_energy_threshold),
+                   gamma_regulator=float(gamma_regulator), delta_regulator=float(delta_regulator),
+                   netCC=float(netCC))
+
+    @classmethod
+    def from_setup(cls, setup: dict):
+        """From the dict of prepare_likelihood_inputs (likelihood_setup.py:207-238)."""
+        return cls.from_arrays(setup["FP_t"], setup["FX_t"], setup["ml"],
+                               setup.get("sky_valid_indices"),
+                               network_energy_threshold=setup["network_energy_threshold"],
+                               gamma_regulator=setup["gamma_regulator"],
+                               delta_regulator=setup["delta_regulator"], netCC=setup["netCC"])
+
+    @property
+    def REG0(self) -> float:
+        """REG[0] = delta * sqrt(2) as float32 (likelihood.py:258)."""
+        return float(np.float32(self.delta_regulator * np.sqrt(2)))
+
+
+class ClusterBatch:
+    """Clusters concatenated along the pixel axis (host, pinned)."""
+
+    def __init__(self, n_ifo: int, n_delay: int, sizes):
+        self.n_ifo, self.n_delay = int(n_ifo), int(n_delay)
+        self.sizes = np.asarray(sizes, dtype=np.int64)
+        self.n_clusters = int(self.sizes.size)
+        self.pix_offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        self.td_offsets = self.pix_offsets * (self.n_delay * self.n_ifo)
+        self.total_pix = int(self.pix_offsets[-1])
+        n_td = self.total_pix * self.n_delay * self.n_ifo
+        self.td00 = torch.empty(n_td, dtype=torch.float32, pin_memory=True)
+        self.td90 = torch.empty(n_td, dtype=torch.float32, pin_memory=True)
+        self.rms = torch.empty((self.total_pix, self.n_ifo), dtype=torch.float32, pin_memory=True)
+
+    @classmethod
+    def from_clusters(cls, clusters):
+        """clusters: iterable of (td00, td90, rms) with the reference's layouts
+        (n_delay, n_ifo, n_pix), (n_delay, n_ifo, n_pix), (n_pix, n_ifo)."""
+        clusters = list(clusters)
+        if not clusters:
+            raise ValueError("empty cluster list")
+        n_delay, n_ifo, _ = np.shape(clusters[0][0])
+        b = cls(n_ifo, n_delay, [np.shape(c[0])[2] for c in clusters])
+        for c, (t0, t9, r) in enumerate(clusters):
+            b.set_cluster(c, t0, t9, r)
+        return b
+
+    def set_cluster(self, c, td00, td90, rms):
+        P = int(self.sizes[c])
+        if (np.shape(td00) != (self.n_delay, self.n_ifo, P) or np.shape(td90) != np.shape(td00)
+                or np.shape(rms) != (P, self.n_ifo)):
+            raise ValueError(f"cluster {c}: td00/td90 must be (n_delay, n_ifo, {P}) and rms "
+                             f"({P}, n_ifo)")
+        a, b = int(self.td_offsets[c]), int(self.td_offsets[c + 1])
+        self.td00[a:b] = torch.from_numpy(np.ascontiguousarray(td00, np.float32).ravel())
+        self.td90[a:b] = torch.from_numpy(np.ascontiguousarray(td90, np.float32).ravel())
+        p0, p1 = int(self.pix_offsets[c]), int(self.pix_offsets[c + 1])
+        self.rms[p0:p1] = torch.from_numpy(np.ascontiguousarray(rms, np.float32))
+
+    def cluster_views(self, c):
+        a, b = int(self.td_offsets[c]), int(self.td_offsets[c + 1])
+        P = int(self.sizes[c])
+        shp = (self.n_delay, self.n_ifo, P)
+        return (self.td00[a:b].numpy().reshape(shp), self.td90[a:b].numpy().reshape(shp),
+                self.rms[int(self.pix_offsets[c]):int(self.pix_offsets[c + 1])].numpy())
+
+    @property
+    def h2d_bytes(self) -> int:
+        return 4 * (self.td00.numel() + self.td90.numel() + self.rms.numel())
+
+
+class BatchedSkyLoop:
+    """Device buffers and launches of the batched sky loop for one batch shape."""
+
+    def __init__(self, tables: SkyTables, batch: ClusterBatch, shape: _lib.TileShape | None = None,
+                 keep_maps: bool = True):
+        if batch.n_ifo != tables.n_ifo:
+            raise ValueError("batch and tables disagree on n_ifo")
+        self.t, self.b = tables, batch
+        self.shape = shape
+        self.L = _lib.load()
+        self.stream = dv.stream()
+        dev = dv.require_cuda()
+        n = batch.n_clusters
+        with torch.cuda.stream(self.stream):
+            self.td00 = torch.empty(batch.td00.numel(), dtype=torch.float32, device=dev)
+            self.td90 = torch.empty(batch.td90.numel(), dtype=torch.float32, device=dev)
+            self.rms = torch.empty(tuple(batch.rms.shape), dtype=torch.float32, device=dev)
+            self.pix_off = torch.from_numpy(batch.pix_offsets).to(dev)
+            self.td_off = torch.from_numpy(batch.td_offsets).to(dev)
+            self.stats = torch.empty((n if keep_maps else 1, N_STATS, tables.n_sky),
+                                     dtype=torch.float32, device=dev)
+            self.res = torch.empty((n, dv.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+            self.regs = torch.empty(n, dtype=torch.float64, device=dev)
+            nbytes = self.L.pgw_workspace_bytes(batch.n_ifo, batch.n_delay, batch.total_pix, n)
+            self.ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        if not keep_maps and n > 1:
+            raise ValueError("keep_maps=False needs the per-cluster maps buffer; not supported")
+        self.res_host = torch.empty((n, dv.RESULT_DTYPE.itemsize), dtype=torch.uint8,
+                                    pin_memory=True)
+        self.regs_host = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        self.graph = None
+
+    # -- steps -------------------------------------------------------------
+    def upload(self):
+        """Host (pinned) -> device copies of the cluster data, async on the stream."""
+        with torch.cuda.stream(self.stream):
+            self.td00.copy_(self.b.td00, non_blocking=True)
+            self.td90.copy_(self.b.td90, non_blocking=True)
+            self.rms.copy_(self.b.rms, non_blocking=True)
+
+    def launch(self):
+        t, b = self.t, self.b
+        rc = self.L.pgw_sky_loop_batched(
+            b.n_ifo, b.n_clusters, self.pix_off.data_ptr(), self.td_off.data_ptr(), b.total_pix,
+            t.n_sky, t.FP.data_ptr(), t.FX.data_ptr(), self.rms.data_ptr(), self.td00.data_ptr(),
+            self.td90.data_ptr(), b.n_delay, t.ml.data_ptr(), t.REG0, t.gamma_regulator, t.netCC,
+            t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(),
+            self.stats.data_ptr(), self.res.data_ptr(), self.regs.data_ptr(),
+            None if self.shape is None else ctypes.byref(self.shape), self.ws.data_ptr(),
+            self.ws.numel(), self.stream.cuda_stream)
+        _lib.check(rc, "sky_loop_batched")
+
+    def download(self):
+        """Device -> host (pinned) copies of the per-cluster results, async."""
+        with torch.cuda.stream(self.stream):
+            self.res_host.copy_(self.res, non_blocking=True)
+            self.regs_host.copy_(self.regs, non_blocking=True)
+
+    @property
+    def d2h_bytes(self) -> int:
+        return self.res_host.numel() + 8 * self.regs_host.numel()
+
+    def capture(self):
+        """Capture launch() in a CUDA graph (after one eager launch)."""
+        self.launch()
+        self.stream.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.stream):
+            self.launch()
+        self.graph = g
+        return g
+
+    def replay(self):
+        """Replay the captured launch on this loop's stream (a CUDAGraph
+        replays on the current stream, so it is made current here)."""
+        if self.graph is None:
+            self.capture()
+        with torch.cuda.stream(self.stream):
+            self.graph.replay()
+
+    def run(self, *, upload=True, download=True):
+        """The public one-call path: upload, launch, download, wait."""
+        if upload:
+            self.upload()
+        self.launch()
+        if download:
+            self.download()
+        self.stream.synchronize()
+        return self.results() if download else None
+
+    # -- results -----------------------------------------------------------
+    def results(self):
+        r = self.res_host.numpy().view(dv.RESULT_DTYPE).reshape(-1)
+        status = int(np.bitwise_or.reduce(r["status"])) if r.size else 0
+        _lib.check_device_status(status, "sky_loop_batched")
+        return BatchResult(l_max=r["l_max"].copy(), sky_stat_max=r["sky_stat_max"].copy(),
+                           found=r["found"].astype(bool), regulator=self.regs_host.numpy().copy(),
+                           maps=self.stats)
+
+
+@dataclass
+class BatchResult:
+    l_max: np.ndarray          # (n_clusters,) int64
+    sky_stat_max: np.ndarray   # (n_clusters,) float32
+    found: np.ndarray          # (n_clusters,) bool: some direction reached the >= comparison
+    regulator: np.ndarray      # (n_clusters,) float64 REG[1]
+    maps: torch.Tensor         # (n_clusters, 11, n_sky) float32 on the device
+
+    def cluster_tuple(self, c):
+        """Cluster c as the reference's 13-tuple (sky_scan.py:191-192)."""
+        st = self.maps[c].cpu().numpy()
+        smax = np.float32(self.sky_stat_max[c]) if self.found[c] else 0
+        return (int(self.l_max[c]),) + tuple(st[k] for k in range(N_STATS)) + (smax,)
+
+
+def sky_loop_batched(tables: SkyTables, clusters, shape=None):
+    """One-shot convenience: evaluate a list of (td00, td90, rms) clusters."""
+    batch = clusters if isinstance(clusters, ClusterBatch) else ClusterBatch.from_clusters(clusters)
+    loop = BatchedSkyLoop(tables, batch, shape=shape)
+    return loop.run()
+
+
+def n_work_items(n_valid: int, n_clusters: int, shape: _lib.TileShape | None) -> int:
+    threads = (shape.threads if shape and shape.threads else 256)
+    lanes = (shape.lanes_per_sky if shape and shape.lanes_per_sky else 1)
+    return 2 * n_clusters * math.ceil(n_valid / (threads // lanes))

@@ -77,3 +77,65 @@ def make_cluster(rng, ml, FP_t, FX_t, n_pix, K, snr, l_true=None, spread=1.5):
 
 def log_uniform_sizes(rng, n, lo, hi):
     return np.exp(rng.uniform(math.log(lo), math.log(hi), size=n)).astype(np.int64)
+
+
+def make_batch_device(seed, sizes, ml, FP_t, FX_t, K, snr_lo=8.0, snr_hi=40.0, spread=1.5,
+                      device="cuda"):
+    """Many clusters at once, generated on the GPU with torch.
+
+    Same model as make_cluster (noise N(0,1), per-pixel weights from
+    s ~ U[0.5, 2], a coherent signal of network SNR ~ U[snr_lo, snr_hi] from
+    an independent random direction per cluster), laid out for
+    ClusterBatch: cluster c's (2K+1, nIFO, P_c) block at td_offsets[c].
+    Returns (td00, td90, rms, l_true, snr) as device tensors / numpy.
+    """
+    import torch
+
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    rng = np.random.default_rng(seed)
+    sizes = np.asarray(sizes, np.int64)
+    n = sizes.size
+    n_ifo, n_sky = ml.shape
+    D = 2 * K + 1
+    P_tot = int(sizes.sum())
+    pix_off = np.concatenate([[0], np.cumsum(sizes)])
+    l_true = rng.integers(n_sky, size=n)
+    snr = rng.uniform(snr_lo, snr_hi, size=n)
+
+    cl = torch.from_numpy(np.repeat(np.arange(n), sizes)).to(dev)           # cluster of pixel
+    j = torch.arange(P_tot, device=dev) - torch.from_numpy(pix_off[:-1]).to(dev)[cl]
+    Pc = torch.from_numpy(sizes).to(dev)[cl]
+    td_base = torch.from_numpy(pix_off[:-1] * D * n_ifo).to(dev)[cl]
+
+    sigma = torch.rand((P_tot, n_ifo), generator=g, device=dev, dtype=torch.float64) * 1.5 + 0.5
+    inv = 1.0 / sigma
+    rms = (inv / torch.sqrt((inv * inv).sum(1, keepdim=True))).to(torch.float32)
+
+    td00 = torch.randn(P_tot * D * n_ifo, generator=g, device=dev, dtype=torch.float32)
+    td90 = torch.randn(P_tot * D * n_ifo, generator=g, device=dev, dtype=torch.float32)
+
+    w = torch.exp(torch.randn(P_tot, generator=g, device=dev, dtype=torch.float64))
+    wsum = torch.zeros(n, device=dev, dtype=torch.float64).index_add_(0, cl, w)
+    w = w / wsum[cl]
+    h = torch.randn((4, P_tot), generator=g, device=dev, dtype=torch.float64) * torch.sqrt(w)
+    lt = torch.from_numpy(l_true).to(dev)[cl]
+    fp = torch.from_numpy(FP_t.astype(np.float64)).to(dev)[lt]             # (P, I)
+    fx = torch.from_numpy(FX_t.astype(np.float64)).to(dev)[lt]
+    r = rms.to(torch.float64)
+    s00 = r * (fp * h[0][:, None] + fx * h[1][:, None])
+    s90 = r * (fp * h[2][:, None] + fx * h[3][:, None])
+    e = torch.zeros(n, device=dev, dtype=torch.float64).index_add_(
+        0, cl, (s00 * s00 + s90 * s90).sum(1))
+    scale = torch.from_numpy(snr).to(dev) / torch.sqrt(torch.clamp(e, min=1e-300))
+    s00 = s00 * scale[cl][:, None]
+    s90 = s90 * scale[cl][:, None]
+    d0 = torch.from_numpy(ml.astype(np.int64).T).to(dev)[lt] + K          # (P, I)
+    for d in range(D):
+        prof = torch.exp(-0.5 * ((d - d0).to(torch.float64) / spread) ** 2)
+        for i in range(n_ifo):
+            idx = td_base + (d * n_ifo + i) * Pc + j
+            td00.index_add_(0, idx, (prof[:, i] * s00[:, i]).to(torch.float32))
+            td90.index_add_(0, idx, (prof[:, i] * s90[:, i]).to(torch.float32))
+    return td00, td90, rms, l_true, snr

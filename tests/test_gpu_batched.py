@@ -1,0 +1,107 @@
+"""Batched sky loop (one persistent launch, work queue) against the oracle.
+
+Each cluster of the batch must reproduce the single-cluster reference loop
+(regulator then scan, likelihood.py:310-325) under the tolerance of
+tests/parity.py; the batched maps must equal the plain per-cluster launch
+exactly (same kernel, same arithmetic, same summation order).
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from parity import assert_scan_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pycwb_gb300 import _lib, sky
+    from pycwb_gb300.likelihoodWP.batched import SkyTables
+    from pycwb_gb300.synthetic import regulators
+    _lib.build()
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(["L1", "H1", "V1"], "L1", 512.0, 20,
+                                                    healpix_order=4)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    reg = regulators(3)
+    tables = SkyTables.from_arrays(FP_t, FX_t, ml, None, **{k: reg[k] for k in (
+        "network_energy_threshold", "gamma_regulator", "delta_regulator", "netCC")})
+    return dict(ml=ml, FP_t=FP_t, FX_t=FX_t, reg=reg, tables=tables)
+
+
+def _clusters(env, sizes, seed):
+    from pycwb_gb300.synthetic import make_cluster
+    rng = np.random.default_rng(seed)
+    out = []
+    for P in sizes:
+        td00, td90, rms, _ = make_cluster(rng, env["ml"], env["FP_t"], env["FX_t"], int(P), 20,
+                                          float(rng.uniform(8, 40)))
+        out.append((td00, td90, rms))
+    return out
+
+
+@pytest.mark.parametrize("spec", [None, (256, 2, 0, 3, 4, 0), (128, 1, 7, 2, 3, 1)])
+def test_batched_matches_oracle_and_plain(env, oracle_mod, spec):
+    from pycwb_gb300._lib import TileShape
+    from pycwb_gb300.likelihoodWP import sky_loop
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch
+
+    shape = None if spec is None else TileShape(*spec)
+    sizes = [20, 350, 1, 77, 0, 130, 20, 512, 3]
+    clusters = _clusters(env, sizes, seed=11)
+    batch = ClusterBatch.from_clusters(clusters)
+    loop = BatchedSkyLoop(env["tables"], batch, shape=shape)
+    res = loop.run()
+    reg, ml, FP_t, FX_t = env["reg"], env["ml"], env["FP_t"], env["FX_t"]
+    n_sky = ml.shape[1]
+    valid = np.arange(n_sky, dtype=np.int64)
+    REG0 = np.float32(reg["delta_regulator"] * math.sqrt(2))
+    for c, (td00, td90, rms) in enumerate(clusters):
+        reg1 = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
+                                        reg["network_energy_threshold"], valid)
+        assert np.float32(res.regulator[c]) == np.float32(reg1)
+        REG = np.array([REG0, reg1, 0.0], np.float32)
+        args = (3, rms.shape[0], n_sky, FP_t, FX_t, rms, td00, td90, ml)
+        tail = (reg["netCC"], reg["delta_regulator"], reg["network_energy_threshold"], valid)
+        ref = oracle_mod.scan_sky_for_best_fit(*args, REG, *tail, return_ellipticity=True)
+        f64 = oracle_mod.scan_sky_for_best_fit(*args, REG.astype(np.float64), *tail,
+                                               precision="f64", return_ellipticity=True)
+        got = res.cluster_tuple(c)
+        assert_scan_close(got, ref, f64, ref_cr=ref[13], netCC=reg["netCC"],
+                          what=f"cluster {c} (P={rms.shape[0]}) shape {spec}")
+        # the plain launch of the same kernel gives identical bits
+        _, plain = sky_loop(*args, REG0, reg["gamma_regulator"], reg["netCC"],
+                            reg["network_energy_threshold"], valid, shape=shape)
+        assert plain[0] == got[0]
+        for k in range(1, 12):
+            np.testing.assert_array_equal(plain[k], got[k])
+
+
+def test_batched_graph_replay_is_repeatable(env):
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch
+
+    import torch
+
+    batch = ClusterBatch.from_clusters(_clusters(env, [40, 300, 5, 999], seed=3))
+    loop = BatchedSkyLoop(env["tables"], batch)
+    first = loop.run()
+    maps0 = loop.stats.clone()
+    loop.capture()
+    for _ in range(3):
+        with torch.cuda.stream(loop.stream):   # wipe every output, then replay
+            loop.stats.fill_(float("nan"))
+            loop.res.zero_()
+            loop.regs.zero_()
+        loop.replay()
+        loop.download()
+        loop.stream.synchronize()
+        again = loop.results()
+        np.testing.assert_array_equal(first.l_max, again.l_max)
+        np.testing.assert_array_equal(first.sky_stat_max, again.sky_stat_max)
+        np.testing.assert_array_equal(first.regulator, again.regulator)
+        assert bool((loop.stats == maps0).all())
