@@ -121,6 +121,30 @@ int pgw_sky_loop(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP, const
                  double* out_regulator, const pgw_tile_shape* shape, void* workspace,
                  size_t workspace_bytes, void* stream);
 
+/* Allocation-free form of pgw_sky_loop.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory per call --
+ * cudaMalloc/cudaFree may synchronise the device, and a host framework that
+ * owns the device memory (its own pool, a fixed budget) may forbid
+ * allocations outside it.  Scratch comes from a static device array of
+ * pgw_sky_loop_noalloc_max_scratch() bytes (8 MiB, enough for about 8,000
+ * pixels at n_ifo = 3 and n_delay = 41) that every GPU loading the library
+ * holds until the process exits; a larger cluster is rejected with
+ * PGW_ERR_WORKSPACE.  The call allocates nothing (no cudaMalloc/cudaFree, no
+ * allocating library routine).  Its first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current:
+ * make that first call before any stream capture.  Every call shares the one
+ * array and leaves its contents behind (each call clears what must start at
+ * zero), so calls that overlap on the GPU -- on different streams or from
+ * different host threads -- race: serialise them.  Inputs and outputs as in
+ * pgw_sky_loop; the default launch shape is used. */
+size_t pgw_sky_loop_noalloc_max_scratch(void);
+int pgw_sky_loop_noalloc(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP,
+                         const float* FX, const float* rms, const float* td00, const float* td90,
+                         int n_delay, const int32_t* ml, float REG0, double gamma_regulator,
+                         double netCC, double network_energy_threshold,
+                         const int64_t* sky_valid_indices, int64_t n_valid, float* out_stats,
+                         pgw_scan_result* out_result, double* out_regulator, void* stream);
+
 /* Regulator and scan for many clusters of one segment in ONE persistent
  * launch driven by a work queue of (cluster, sky tile) items taken in
  * decreasing cluster size.  Replaces the per-cluster loop of

@@ -100,6 +100,10 @@ def load():
                                            f64, f64, f64, P, i64, P, P, P, P, P, sz, P]
         L.pgw_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, P, i32, i32, i32, i32, P, P]
         L.pgw_fp32_fma_peak.argtypes = [i32, P, P, P]
+        L.pgw_sky_loop_noalloc.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64,
+                                           f64, P, i64, P, P, P, P]
+        L.pgw_sky_loop_noalloc.restype = ctypes.c_int
+        L.pgw_sky_loop_noalloc_max_scratch.restype = sz
         for name in ("pgw_fp32_fma_peak", "pgw_calculate_dpf", "pgw_scan_sky_for_best_fit", "pgw_sky_loop",
                      "pgw_sky_loop_batched", "pgw_batch_get_td_vecs"):
             getattr(L, name).restype = ctypes.c_int
