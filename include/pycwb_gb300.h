@@ -53,7 +53,9 @@ typedef struct {
   int32_t found;        /* 0: no valid direction reached the >= comparison; l_max = valid[0] */
   int32_t status;       /* OR of (1 << pgw_status) for device-detected errors */
   float regulator;      /* REG[1] used by the scan (float32, as stored by likelihood.py:310) */
-} pgw_scan_result;
+  int64_t active_pairs; /* (direction, pixel) pairs above the energy threshold: sum over the
+                           valid directions of the pixel count NN of sky_stat.py:184 */
+} pgw_scan_result;      /* 32 bytes */
 
 /* Library version string. */
 const char* pgw_version(void);
@@ -64,6 +66,18 @@ const char* pgw_last_error(void);
 /* Bytes of scratch a call needs for n_clusters clusters holding total_pix
  * pixels in all (plain calls: n_clusters = 1, total_pix = n_pix). */
 size_t pgw_workspace_bytes(int n_ifo, int n_delay, int64_t total_pix, int n_clusters);
+
+/* Scan order of the valid directions (host arrays, once per segment):
+ * out_order[0..n_valid) = positions of sky_valid_indices sorted by their
+ * delay tuple (ml[0, l], ..., ml[n_ifo-1, l]), ties in position order;
+ * *out_n_tuples = number of distinct tuples.  Directions with one tuple see
+ * the same delayed data and so the same pixel energy mask; passed as
+ * `sky_order` to the sky-loop calls, it lets a warp evaluate only the pixels
+ * above the energy threshold.  Results do not depend on the order (the sky
+ * maximum's tie rule uses the positions in sky_valid_indices).  Counterpart
+ * of nothing in the reference (an execution order, not a result). */
+int pgw_sky_order(const int32_t* ml, int n_ifo, int64_t n_sky, const int64_t* sky_valid_indices,
+                  int64_t n_valid, int32_t* out_order, int64_t* out_n_tuples);
 
 /* DPF regulator: REG[1] = (n_valid^2 / (n_pass^2 + 1e-9) - 1) * E_thr, where
  * n_pass counts valid directions whose DPF quality sqrt(NI / (NN + 0.01))
@@ -80,13 +94,15 @@ int pgw_calculate_dpf(const float* FP, const float* FX, const float* rms, int64_
 /* Sky scan over the valid directions with a given REG (device, 3 floats).
  * Replaces scan_sky_for_best_fit, pycwb/modules/likelihoodWP/sky_scan.py:17-192.
  * out_stats: (11, n_sky) float32; entries of directions that are masked or
- * rejected are 0, as in the reference. */
+ * rejected are 0, as in the reference.  sky_order: device int32 array from
+ * pgw_sky_order (n_valid entries), or NULL to scan in the given order. */
 int pgw_scan_sky_for_best_fit(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP,
                               const float* FX, const float* rms, const float* td00,
                               const float* td90, int n_delay, const int32_t* ml, const float* REG,
                               double netCC, double delta_regulator,
                               double network_energy_threshold,
-                              const int64_t* sky_valid_indices, int64_t n_valid, float* out_stats,
+                              const int64_t* sky_valid_indices, int64_t n_valid,
+                              const int32_t* sky_order, float* out_stats,
                               pgw_scan_result* out_result, void* workspace, size_t workspace_bytes,
                               void* stream);
 
@@ -117,9 +133,10 @@ int pgw_sky_loop(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP, const
                  const float* rms, const float* td00, const float* td90, int n_delay,
                  const int32_t* ml, float REG0, double gamma_regulator, double netCC,
                  double network_energy_threshold, const int64_t* sky_valid_indices,
-                 int64_t n_valid, float* out_stats, pgw_scan_result* out_result,
-                 double* out_regulator, const pgw_tile_shape* shape, void* workspace,
-                 size_t workspace_bytes, void* stream);
+                 int64_t n_valid, const int32_t* sky_order, float* out_stats,
+                 pgw_scan_result* out_result, double* out_regulator,
+                 const pgw_tile_shape* shape, void* workspace, size_t workspace_bytes,
+                 void* stream);
 
 /* Allocation-free form of pgw_sky_loop.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory per call --
@@ -142,8 +159,9 @@ int pgw_sky_loop_noalloc(int n_ifo, int64_t n_pix, int64_t n_sky, const float* F
                          const float* FX, const float* rms, const float* td00, const float* td90,
                          int n_delay, const int32_t* ml, float REG0, double gamma_regulator,
                          double netCC, double network_energy_threshold,
-                         const int64_t* sky_valid_indices, int64_t n_valid, float* out_stats,
-                         pgw_scan_result* out_result, double* out_regulator, void* stream);
+                         const int64_t* sky_valid_indices, int64_t n_valid,
+                         const int32_t* sky_order, float* out_stats, pgw_scan_result* out_result,
+                         double* out_regulator, void* stream);
 
 /* Regulator and scan for many clusters of one segment in ONE persistent
  * launch driven by a work queue of (cluster, sky tile) items taken in
@@ -162,9 +180,10 @@ int pgw_sky_loop_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                          const float* td00_all, const float* td90_all, int n_delay,
                          const int32_t* ml, float REG0, double gamma_regulator, double netCC,
                          double network_energy_threshold, const int64_t* sky_valid_indices,
-                         int64_t n_valid, float* out_stats, pgw_scan_result* out_results,
-                         double* out_regulators, const pgw_tile_shape* shape, void* workspace,
-                         size_t workspace_bytes, void* stream);
+                         int64_t n_valid, const int32_t* sky_order, float* out_stats,
+                         pgw_scan_result* out_results, double* out_regulators,
+                         const pgw_tile_shape* shape, void* workspace, size_t workspace_bytes,
+                         void* stream);
 
 /* td-amplitude vectors of n_pixels pixels of one (layer, detector) plane:
  * out (n_pixels, 4K+2) float32 = [a00(-K..K), a90(-K..K)] per pixel.

@@ -15,8 +15,8 @@ import numpy as np
 import torch
 
 RESULT_DTYPE = np.dtype([("l_max", "<i8"), ("sky_stat_max", "<f4"), ("found", "<i4"),
-                         ("status", "<i4"), ("regulator", "<f4")])
-assert RESULT_DTYPE.itemsize == 24
+                         ("status", "<i4"), ("regulator", "<f4"), ("active_pairs", "<i8")])
+assert RESULT_DTYPE.itemsize == 32
 
 _tls = threading.local()
 

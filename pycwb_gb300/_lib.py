@@ -93,15 +93,17 @@ def load():
         L.pgw_workspace_bytes.restype = sz
         L.pgw_calculate_dpf.argtypes = [P, P, P, i64, i32, i64, f64, f64, P, i64, P, P, P, sz, P]
         L.pgw_scan_sky_for_best_fit.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, P, f64, f64,
-                                                f64, P, i64, P, P, P, sz, P]
+                                                f64, P, i64, P, P, P, P, sz, P]
         L.pgw_sky_loop.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64, f64, P,
-                                   i64, P, P, P, P, P, sz, P]
+                                   i64, P, P, P, P, P, P, sz, P]
         L.pgw_sky_loop_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
-                                           f64, f64, f64, P, i64, P, P, P, P, P, sz, P]
+                                           f64, f64, f64, P, i64, P, P, P, P, P, P, sz, P]
+        L.pgw_sky_order.argtypes = [P, i32, i64, P, i64, P, P]
+        L.pgw_sky_order.restype = ctypes.c_int
         L.pgw_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, P, i32, i32, i32, i32, P, P]
         L.pgw_fp32_fma_peak.argtypes = [i32, P, P, P]
         L.pgw_sky_loop_noalloc.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64,
-                                           f64, P, i64, P, P, P, P]
+                                           f64, P, i64, P, P, P, P, P]
         L.pgw_sky_loop_noalloc.restype = ctypes.c_int
         L.pgw_sky_loop_noalloc_max_scratch.restype = sz
         for name in ("pgw_fp32_fma_peak", "pgw_calculate_dpf", "pgw_scan_sky_for_best_fit", "pgw_sky_loop",
@@ -120,6 +122,19 @@ class TileShape(ctypes.Structure):
     def key(self):
         return (self.threads, self.lanes_per_sky, self.chunk_pix, self.stages, self.min_blocks,
                 self.fast_math)
+
+
+def sky_order(ml, sky_valid_indices):
+    """Scan order of the valid directions grouped by delay tuple (host int32)."""
+    import numpy as np
+    ml = np.ascontiguousarray(ml, dtype=np.int32)
+    valid = np.ascontiguousarray(sky_valid_indices, dtype=np.int64)
+    out = np.empty(valid.size, dtype=np.int32)
+    n_t = ctypes.c_int64(0)
+    rc = load().pgw_sky_order(ml.ctypes.data, ml.shape[0], ml.shape[1], valid.ctypes.data,
+                              valid.size, out.ctypes.data, ctypes.byref(n_t))
+    check(rc, "sky_order")
+    return out, int(n_t.value)
 
 
 STATUS_NAMES = {

@@ -32,8 +32,9 @@ _lock = threading.Lock()
 def candidates(n_ifo: int, fast_math: bool):
     out = []
     minbs = (3, 4) if n_ifo <= 4 else (2,)
-    for threads, lanes, stages, minb in itertools.product((128, 256), (1, 2, 4), (2, 3, 4), minbs):
-        out.append(_lib.TileShape(threads, lanes, 0, stages, minb, int(fast_math)))
+    for threads, lanes, stages, chunk, minb in itertools.product((128, 256), (1, 2), (2, 3),
+                                                                  (0, 16), minbs):
+        out.append(_lib.TileShape(threads, lanes, chunk, stages, minb, int(fast_math)))
     return out
 
 

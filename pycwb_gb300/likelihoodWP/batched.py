@@ -37,6 +37,8 @@ class SkyTables:
     FX: torch.Tensor
     ml: torch.Tensor
     valid: torch.Tensor
+    order: torch.Tensor          # scan order of valid positions grouped by delay tuple
+    n_tuples: int
     n_ifo: int
     n_sky: int
     network_energy_threshold: float
@@ -52,9 +54,15 @@ class SkyTables:
             raise ValueError("FP/FX must be (n_sky, n_ifo) and ml (n_ifo, n_sky)")
         if sky_valid_indices is None:
             sky_valid_indices = np.arange(n_sky, dtype=np.int64)
+        ml_h = ml.cpu().numpy() if isinstance(ml, torch.Tensor) else np.asarray(ml)
+        v_h = (sky_valid_indices.cpu().numpy() if isinstance(sky_valid_indices, torch.Tensor)
+               else np.asarray(sky_valid_indices))
+        order, n_tuples = _lib.sky_order(ml_h, v_h)
         return cls(FP=dv.to_device(FP_t, torch.float32), FX=dv.to_device(FX_t, torch.float32),
                    ml=dv.to_device(ml, torch.int32),
-                   valid=dv.to_device(sky_valid_indices, torch.int64), n_ifo=int(n_ifo),
+                   valid=dv.to_device(sky_valid_indices, torch.int64),
+                   order=dv.to_device(order, torch.int32), n_tuples=int(n_tuples),
+                   n_ifo=int(n_ifo),
                    n_sky=int(n_sky), network_energy_threshold=float(network_energy_threshold),
                    gamma_regulator=float(gamma_regulator), delta_regulator=float(delta_regulator),
                    netCC=float(netCC))
@@ -172,7 +180,7 @@ class BatchedSkyLoop:
             b.n_ifo, b.n_clusters, self.pix_off.data_ptr(), self.td_off.data_ptr(), b.total_pix,
             t.n_sky, t.FP.data_ptr(), t.FX.data_ptr(), self.rms.data_ptr(), self.td00.data_ptr(),
             self.td90.data_ptr(), b.n_delay, t.ml.data_ptr(), t.REG0, t.gamma_regulator, t.netCC,
-            t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(),
+            t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(), t.order.data_ptr(),
             self.stats.data_ptr(), self.res.data_ptr(), self.regs.data_ptr(),
             None if self.shape is None else ctypes.byref(self.shape), self.ws.data_ptr(),
             self.ws.numel(), self.stream.cuda_stream)
@@ -223,7 +231,7 @@ class BatchedSkyLoop:
         _lib.check_device_status(status, "sky_loop_batched")
         return BatchResult(l_max=r["l_max"].copy(), sky_stat_max=r["sky_stat_max"].copy(),
                            found=r["found"].astype(bool), regulator=self.regs_host.numpy().copy(),
-                           maps=self.stats)
+                           maps=self.stats, active_pairs=r["active_pairs"].copy())
 
 
 @dataclass
@@ -233,6 +241,7 @@ class BatchResult:
     found: np.ndarray          # (n_clusters,) bool: some direction reached the >= comparison
     regulator: np.ndarray      # (n_clusters,) float64 REG[1]
     maps: torch.Tensor         # (n_clusters, 11, n_sky) float32 on the device
+    active_pairs: np.ndarray   # (n_clusters,) int64 (direction, pixel) pairs above E_thr
 
     def cluster_tuple(self, c):
         """Cluster c as the reference's 13-tuple (sky_scan.py:191-192)."""

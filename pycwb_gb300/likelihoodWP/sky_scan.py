@@ -36,6 +36,34 @@ def _check_tables(FP, FX, rms, n_sky, n_ifo):
             f"got FP: {dv.shape_of(FP)}, FX: {dv.shape_of(FX)}, rms: {dv.shape_of(rms)}")
 
 
+_order_cache = {}
+
+
+def _sky_order_device(ml, sky_valid_indices, device):
+    """Scan order grouped by delay tuple (pgw_sky_order), cached per (ml, valid) pair.
+
+    The order only groups directions for speed; results do not depend on it,
+    so a cache hit on arrays changed in place costs time, never correctness."""
+    def ident(x):
+        if isinstance(x, torch.Tensor):
+            return ("t", x.data_ptr(), tuple(x.shape))
+        a = np.asarray(x)
+        return ("n", id(x), a.__array_interface__["data"][0], a.shape)
+    key = (ident(ml), ident(sky_valid_indices))
+    hit = _order_cache.get(key)
+    if hit is not None:
+        return hit
+    ml_h = ml.cpu().numpy() if isinstance(ml, torch.Tensor) else np.asarray(ml)
+    v_h = (sky_valid_indices.cpu().numpy() if isinstance(sky_valid_indices, torch.Tensor)
+           else np.asarray(sky_valid_indices))
+    order, _ = _lib.sky_order(ml_h, v_h)
+    t = torch.from_numpy(order).to(device)
+    if len(_order_cache) > 16:
+        _order_cache.clear()
+    _order_cache[key] = t
+    return t
+
+
 def _valid(sky_valid_indices, n_sky):
     v = dv.to_device(sky_valid_indices, torch.int64)
     if v.ndim != 1 or v.numel() == 0:
@@ -103,6 +131,7 @@ def scan_sky_for_best_fit(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG,
     REGd = dv.to_device(np.asarray(REG, np.float32) if not isinstance(REG, torch.Tensor) else REG,
                         torch.float32)
     valid = _valid(sky_valid_indices, n_sky)
+    order = _sky_order_device(ml, sky_valid_indices, FPd.device)
     ws = dv.workspace(L.pgw_workspace_bytes(n_ifo, n_delay, n_pix, 1))
     with torch.cuda.stream(s):
         stats = torch.empty((N_STATS, n_sky), dtype=torch.float32, device=FPd.device)
@@ -111,18 +140,20 @@ def scan_sky_for_best_fit(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG,
                                      rmsd.data_ptr(), t0.data_ptr(), t9.data_ptr(), n_delay,
                                      mld.data_ptr(), REGd.data_ptr(), float(netCC),
                                      float(delta_regulator), float(network_energy_threshold),
-                                     valid.data_ptr(), valid.numel(), stats.data_ptr(),
-                                     res.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     valid.data_ptr(), valid.numel(), order.data_ptr(),
+                                     stats.data_ptr(), res.data_ptr(), ws.data_ptr(), ws.numel(),
                                      dv.stream_handle(s))
     _lib.check(rc, "scan_sky_for_best_fit")
     return _scan_outputs(stats, res, return_device, s)
 
 
 def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regulator, netCC,
-             network_energy_threshold, sky_valid_indices, *, shape=None, return_device=False):
+             network_energy_threshold, sky_valid_indices, *, shape=None, sky_order=True,
+             return_device=False):
     """Regulator + scan of one cluster in one launch (likelihood.py:308-325).
 
     Returns (regulator, scan 13-tuple); REG = [REG0, float32(regulator), 0].
+    sky_order=False scans the directions in the given order (same results).
     """
     n_ifo, n_pix, n_sky = int(n_ifo), int(n_pix), int(n_sky)
     _check_tables(FP, FX, rms, n_sky, n_ifo)
@@ -136,6 +167,7 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     t0, t9 = dv.to_device(td00, torch.float32), dv.to_device(td90, torch.float32)
     mld = dv.to_device(ml, torch.int32)
     valid = _valid(sky_valid_indices, n_sky)
+    order = _sky_order_device(ml, sky_valid_indices, FPd.device) if sky_order else None
     ws = dv.workspace(L.pgw_workspace_bytes(n_ifo, n_delay, n_pix, 1))
     with torch.cuda.stream(s):
         stats = torch.empty((N_STATS, n_sky), dtype=torch.float32, device=FPd.device)
@@ -144,7 +176,7 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     rc = L.pgw_sky_loop(n_ifo, n_pix, n_sky, FPd.data_ptr(), FXd.data_ptr(), rmsd.data_ptr(),
                         t0.data_ptr(), t9.data_ptr(), n_delay, mld.data_ptr(), float(np.float32(REG0)),
                         float(gamma_regulator), float(netCC), float(network_energy_threshold),
-                        valid.data_ptr(), valid.numel(), stats.data_ptr(), res.data_ptr(),
+                        valid.data_ptr(), valid.numel(), dv.ptr(order), stats.data_ptr(), res.data_ptr(),
                         reg.data_ptr(), None if shape is None else ctypes.byref(shape),
                         ws.data_ptr(), ws.numel(), dv.stream_handle(s))
     _lib.check(rc, "sky_loop")

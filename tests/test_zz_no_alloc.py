@@ -49,13 +49,13 @@ def test_noalloc_entry_point_matches_workspace_entry_point_twice():
 
     def outputs():
         return (torch.empty((11, n_sky), dtype=torch.float32, device=dev),
-                torch.zeros(24, dtype=torch.uint8, device=dev),
+                torch.zeros(32, dtype=torch.uint8, device=dev),
                 torch.zeros(1, dtype=torch.float64, device=dev))
 
     common = (3, P, n_sky, t["FP"].data_ptr(), t["FX"].data_ptr(), t["rms"].data_ptr(),
               t["td00"].data_ptr(), t["td90"].data_ptr(), 2 * K + 1, t["ml"].data_ptr(), REG0,
               reg["gamma_regulator"], reg["netCC"], reg["network_energy_threshold"],
-              t["valid"].data_ptr(), n_sky)
+              t["valid"].data_ptr(), n_sky, None)
 
     # the entry point with a caller workspace
     st_ref, res_ref, reg_ref = outputs()
@@ -65,7 +65,7 @@ def test_noalloc_entry_point_matches_workspace_entry_point_twice():
     assert rc == 0, L.pgw_last_error()
     torch.cuda.synchronize()
     ref = res_ref.cpu().numpy().view(np.dtype([("l", "<i8"), ("s", "<f4"), ("f", "<i4"),
-                                               ("st", "<i4"), ("r", "<f4")]))[0]
+                                               ("st", "<i4"), ("r", "<f4"), ("a", "<i8")]))[0]
     assert ref["st"] == 0
 
     # the allocation-free entry point, twice in a row
@@ -98,7 +98,7 @@ def test_noalloc_refuses_a_cluster_larger_than_its_scratch():
     one = torch.zeros(64, dtype=torch.float32, device="cuda")
     p = one.data_ptr()
     rc = L.pgw_sky_loop_noalloc(3, too_many, 12, p, p, p, p, p, 41, p, 0.7, 0.1, 0.5, 12.0, p, 12,
-                                p, p, p, torch.cuda.current_stream().cuda_stream)
+                                None, p, p, p, torch.cuda.current_stream().cuda_stream)
     assert rc == 4  # PGW_ERR_WORKSPACE, nothing launched
     msg = L.pgw_last_error().decode()
     assert "scratch" in msg and str(cap) in msg
