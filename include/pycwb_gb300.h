@@ -198,6 +198,38 @@ int pgw_batch_get_td_vecs(const int32_t* pixel_indices, int64_t n_pixels, const 
                           const double* phase, int M, int n_coeffs, int K, int J, float* out,
                           void* stream);
 
+/* Sky statistic at continuous directions and its gradient (no counterpart
+ * in the reference, which evaluates the statistic only on the grid).  For
+ * query q: cluster query_cluster[q] of the concatenated batch (layouts as in
+ * pgw_sky_loop_batched), direction (theta[q], phi[q]) in radians (Earth-fixed
+ * colatitude and longitude).  F+/Fx come from each detector's response
+ * tensor and the delays tau_i = n . b_i are interpolated linearly between td
+ * samples.  geometry: (n_ifo, 12) float32 = response tensor (row major, 9)
+ * and baseline to the reference detector in TD samples (3).  reg1: REG[1]
+ * per cluster.  out: (n_queries, 8) float32 = statistic (likelihood x
+ * correlation, sky_scan.py:140), d/dtheta, d/dphi, likelihood, correlation,
+ * ellipticity, coherent energy, null energy.  The gradient is exact
+ * (dual-number tangents through the whole pipeline), one-sided at kinks. */
+int pgw_sky_stat_grad(int n_ifo, int n_queries, const int32_t* query_cluster,
+                      const double* theta, const double* phi, const int64_t* pix_offsets,
+                      const int64_t* td_offsets, const float* rms_all, const float* td00_all,
+                      const float* td90_all, int n_delay, const float* geometry, float REG0,
+                      const float* reg1, double network_energy_threshold, float* out,
+                      void* stream);
+
+/* Off-grid refinement of sky maxima: for each query, n_steps of gradient
+ * ascent on the statistic from (theta0, phi0), steps of step0 radians of arc
+ * along the gradient, halved whenever a step would lower the statistic.
+ * Writes the final direction (theta_out, phi_out), its 8 outputs as in
+ * pgw_sky_stat_grad, and (when trace != NULL) (statistic, theta, phi) after
+ * each step: (n_queries, n_steps + 1, 3). */
+int pgw_refine_sky(int n_ifo, int n_queries, const int32_t* query_cluster, const double* theta0,
+                   const double* phi0, const int64_t* pix_offsets, const int64_t* td_offsets,
+                   const float* rms_all, const float* td00_all, const float* td90_all,
+                   int n_delay, const float* geometry, float REG0, const float* reg1,
+                   double network_energy_threshold, int n_steps, float step0, double* theta_out,
+                   double* phi_out, float* out, float* trace, void* stream);
+
 /* Diagnostics (no counterpart in the reference).  Measures the device's
  * FP32 fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) with one
  * timed launch of `iters` x 128 register FMAs per thread; the sky loop's

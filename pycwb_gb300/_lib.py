@@ -19,7 +19,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
-SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu"]
+SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu"]
 HEADERS = ["common.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -99,6 +99,11 @@ def load():
         L.pgw_sky_loop_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
                                            f64, f64, f64, P, i64, P, P, P, P, P, P, sz, P]
         L.pgw_sky_order.argtypes = [P, i32, i64, P, i64, P, P]
+        L.pgw_sky_stat_grad.argtypes = [i32, i32, P, P, P, P, P, P, P, P, i32, P, f32, P, f64, P, P]
+        L.pgw_sky_stat_grad.restype = ctypes.c_int
+        L.pgw_refine_sky.argtypes = [i32, i32, P, P, P, P, P, P, P, P, i32, P, f32, P, f64, i32, f32,
+                                     P, P, P, P, P]
+        L.pgw_refine_sky.restype = ctypes.c_int
         L.pgw_sky_order.restype = ctypes.c_int
         L.pgw_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, P, i32, i32, i32, i32, P, P]
         L.pgw_fp32_fma_peak.argtypes = [i32, P, P, P]
