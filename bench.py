@@ -133,8 +133,9 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend=backend)
         pg = dist
     return world, rank, local, pg
@@ -223,6 +224,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-td", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one eager launch of the batched loop and exit (for ncu)")
     args = ap.parse_args()
@@ -366,12 +369,6 @@ def main():
     achieved = useful_ops / (kernel_ms * 1e-3) / 1e12
     traffic = traffic_from_profile(args.clusters, total_pix)
 
-    # ---- plain: one launch per cluster on the same device data ------------
-    plain = None
-    if not args.no_plain:
-        plain = time_plain(L, loop, tables, batch, shape, dev)
-        plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
-
     # ---- end to end through the public API ------------------------------
     e2e = None
     if not args.no_e2e:
@@ -386,6 +383,15 @@ def main():
         e2e = {"value": world * work_evals / dt, "unit": UNIT,
                "h2d_bytes_per_step": batch.h2d_bytes, "d2h_bytes_per_step": loop.d2h_bytes,
                "ms_per_step": dt * 1e3, "steps": n_e2e, "api": "BatchedSkyLoop.run"}
+
+    # ---- plain: one launch per cluster on the same device data ------------
+    plain = None
+    if not args.no_plain:
+        plain = time_plain(L, loop, tables, batch, shape, dev)
+        plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
+
+    adjoint = time_adjoint(loop, res, batch, args.order, dev) if not args.no_adjoint else None
+    td_build = time_td_build(dev) if not args.no_td else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -425,6 +431,8 @@ def main():
             "clocks": clk,
             "plain": plain,
             "batched_vs_plain": (plain["ms"] / ms_per_step) if plain else None,
+            "adjoint": adjoint,
+            "td_build": td_build,
             "selected": {"found": int(res.found.sum()),
                          "l_max_equals_injected": int(np.sum(res.l_max == l_true))},
             "step_ms": step_ms,
@@ -455,6 +463,67 @@ def traffic_from_profile(n_clusters, total_pix):
                 float(p["read_bytes_per_pixel"]) * total_pix)
     except (OSError, ValueError, KeyError):
         return None
+
+
+def time_adjoint(loop, res, batch, order, dev):
+    """Off-grid refinement of up to 256 clusters of 200-2000 pixels (10 ascent
+    steps each, one launch) from their grid maxima; timed with CUDA events."""
+    import torch
+    from pycwb_gb300.adjoint import GradInputs, detector_geometry, grid_angles, refine
+
+    sel = np.flatnonzero((batch.sizes >= 200) & (batch.sizes <= 2000) & res.found)[:256]
+    if sel.size == 0:
+        return None
+    inp = GradInputs.from_loop(loop, detector_geometry(IFOS, IFOS[0], 512.0), res.regulator)
+    theta, phi = grid_angles(loop.t.n_sky, order)
+    args = (inp, res.l_max[sel], theta, phi, res.sky_stat_max[sel])
+    refine(*args, n_steps=10, healpix_order=order, clusters=sel)  # warm-up
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(loop.stream)
+    r = refine(*args, n_steps=10, healpix_order=order, clusters=sel)
+    e1.record(loop.stream)
+    e1.synchronize()
+    gain = (r.statistic - r.start_statistic) / np.maximum(np.abs(r.start_statistic), 1e-30)
+    return {"clusters": int(sel.size), "steps": 10, "ms": e0.elapsed_time(e1),
+            "improved": int(r.improved.sum()),
+            "median_relative_gain": float(np.median(gain[r.improved])) if r.improved.any() else 0.0,
+            "median_shift_rad": float(np.median(r.distance[r.improved])) if r.improved.any() else 0.0,
+            "evaluations": int(sel.size) * 11,
+            "note": "statistic and (theta, phi) gradient at continuous directions, "
+                    "grid maximum kept where refinement does not beat it"}
+
+
+def time_td_build(dev, n_pix=1_000_000, M=64, nc=20, K=20):
+    """td-amplitude vectors (pgw_batch_get_td_vecs) of n_pix random pixels of one
+    (M+1)-layer plane, K = 20, TD filters of 2*nc+1 taps; CUDA-event timed."""
+    import torch
+    from pycwb_gb300.utils.td_vector_kernels import batch_get_td_vecs
+
+    rng = np.random.default_rng(1)
+    n_time = 4096
+    rows = n_time + 2 * nc
+    p00 = torch.zeros((rows, M + 1), dtype=torch.float32, device=dev)
+    p90 = torch.zeros_like(p00)
+    p00[nc:nc + n_time] = torch.randn((n_time, M + 1), device=dev)
+    p90[nc:nc + n_time] = torch.randn((n_time, M + 1), device=dev)
+    T0 = torch.randn((2 * M + 1, 2 * nc + 1), dtype=torch.float64, device=dev)
+    Tx = torch.randn((2 * M + 1, 2 * nc + 1), dtype=torch.float64, device=dev)
+    idx = torch.from_numpy(rng.integers(0, n_time * (M + 1), n_pix).astype(np.int32)).to(dev)
+    from pycwb_gb300 import _device as dv
+    batch_get_td_vecs(idx, p00, p90, T0, Tx, M, nc, K, M, return_device=True)  # warm-up
+    torch.cuda.synchronize()
+    s = dv.stream()                  # the stream the library launches on
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    batch_get_td_vecs(idx, p00, p90, T0, Tx, M, nc, K, M, return_device=True)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"pixels": n_pix, "layers": M, "K": K, "taps": 2 * nc + 1, "ms": ms,
+            "pixels_per_s": n_pix / (ms * 1e-3),
+            "note": "float64 accumulation, bit-identical to the reference"}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):

@@ -36,6 +36,23 @@ def stream() -> torch.cuda.Stream:
     return s
 
 
+def begin() -> torch.cuda.Stream:
+    """This thread's stream, ordered after the caller's current stream, so
+    device inputs the caller produced on its stream are complete."""
+    s = stream()
+    s.wait_stream(torch.cuda.current_stream())
+    return s
+
+
+def end(s: torch.cuda.Stream, *outputs: torch.Tensor) -> None:
+    """Order the caller's current stream after `s` and tie `outputs` to it."""
+    cur = torch.cuda.current_stream()
+    cur.wait_stream(s)
+    for t in outputs:
+        if isinstance(t, torch.Tensor) and t.is_cuda:
+            t.record_stream(cur)
+
+
 def workspace(nbytes: int) -> torch.Tensor:
     """This thread's scratch buffer, grown on demand (256-byte aligned)."""
     ws = getattr(_tls, "ws", None)
@@ -51,6 +68,7 @@ def to_device(x, dtype: torch.dtype) -> torch.Tensor:
     dev = require_cuda()
     if isinstance(x, torch.Tensor):
         if x.device.type == "cuda" and x.dtype == dtype and x.is_contiguous():
+            x.record_stream(stream())  # used on this thread's stream from here on
             return x
         with torch.cuda.stream(stream()):
             return x.to(device=dev, dtype=dtype).contiguous()

@@ -79,7 +79,7 @@ class GradInputs:
 def sky_stat_grad(inp: GradInputs, query_cluster, theta, phi) -> torch.Tensor:
     """(n_queries, 8) float32 on the device (see OUT_NAMES)."""
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     qc = dv.to_device(query_cluster, torch.int32)
     th = dv.to_device(theta, torch.float64)
     ph = dv.to_device(phi, torch.float64)
@@ -92,7 +92,7 @@ def sky_stat_grad(inp: GradInputs, query_cluster, theta, phi) -> torch.Tensor:
                              inp.geom.data_ptr(), inp.REG0, inp.reg1.data_ptr(),
                              inp.network_energy_threshold, out.data_ptr(), s.cuda_stream)
     _lib.check(rc, "sky_stat_grad")
-    torch.cuda.current_stream().wait_stream(s)
+    dv.end(s, out)
     return out
 
 
@@ -114,29 +114,45 @@ class SkyStatistic(torch.autograd.Function):
 
 @dataclass
 class Refined:
-    theta: np.ndarray        # final direction (grid direction where refinement lost)
+    theta: np.ndarray        # refined direction, or the grid direction where refinement failed
     phi: np.ndarray
-    statistic: np.ndarray    # statistic at the returned direction
-    grid_statistic: np.ndarray
-    improved: np.ndarray     # bool: the off-grid direction beat the grid maximum
+    statistic: np.ndarray    # continuous statistic at the returned direction
+    start_statistic: np.ndarray  # continuous statistic at the grid maximum
+    grid_statistic: np.ndarray   # the grid scan's sky_stat_max (reported detection statistic)
+    improved: np.ndarray     # bool: refinement moved to a better direction near the grid cell
+    distance: np.ndarray     # arc between the grid direction and the refined one (radians)
     trace: np.ndarray        # (n, n_steps + 1, 3) statistic, theta, phi
 
 
+def _arc(t1, p1, t2, p2):
+    c = np.cos(t1) * np.cos(t2) + np.sin(t1) * np.sin(t2) * np.cos(p1 - p2)
+    return np.arccos(np.clip(c, -1.0, 1.0))
+
+
 def refine(inp: GradInputs, l_max, grid_theta, grid_phi, grid_stat, n_steps=10,
-           step0=None, healpix_order=7):
-    """Gradient ascent from each cluster's grid maximum; the grid result is the
-    fallback and the judge: an off-grid direction is kept only if its
-    statistic is at least the grid maximum's (sky_stat_max)."""
+           step0=None, healpix_order=7, clusters=None, max_cells=2.0):
+    """Off-grid refinement of each cluster's grid maximum.
+
+    Gradient ascent on the continuous statistic starts at the grid maximum
+    l_max.  The grid result is the fallback and the judge: the refined
+    direction is kept only if its statistic beats the continuous statistic
+    at the grid direction and it lies within `max_cells` grid spacings of
+    it; otherwise the grid direction is returned.  The grid scan's
+    sky_stat_max stays the detection statistic (`grid_statistic`).
+    `clusters` maps each query to its cluster in the batch (default: query
+    i is cluster i)."""
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     n = len(l_max)
-    if step0 is None:  # half the grid spacing: sqrt(4 pi / 12 / 4^order) / 2
-        step0 = 0.5 * math.sqrt(4 * math.pi / (12 * 4 ** healpix_order))
+    spacing = math.sqrt(4 * math.pi / (12 * 4 ** healpix_order))
+    if step0 is None:
+        step0 = 0.5 * spacing
     th0 = np.asarray(grid_theta, np.float64)[np.asarray(l_max)]
     ph0 = np.asarray(grid_phi, np.float64)[np.asarray(l_max)]
     dev = inp.td00.device
     with torch.cuda.stream(s):
-        qc = torch.arange(n, dtype=torch.int32, device=dev)
+        qc = (torch.arange(n, dtype=torch.int32, device=dev) if clusters is None else
+              torch.as_tensor(np.asarray(clusters, np.int32)).to(dev))
         t0 = torch.from_numpy(th0).to(dev)
         p0 = torch.from_numpy(ph0).to(dev)
         to = torch.empty(n, dtype=torch.float64, device=dev)
@@ -154,8 +170,10 @@ def refine(inp: GradInputs, l_max, grid_theta, grid_phi, grid_stat, n_steps=10,
     with torch.cuda.stream(s):
         o = out.cpu().numpy()
         tt, pp, trace = to.cpu().numpy(), po.cpu().numpy(), tr.cpu().numpy()
-    grid_stat = np.asarray(grid_stat, np.float64)
-    improved = o[:, 0] >= grid_stat
+    start = trace[:, 0, 0].astype(np.float64)
+    dist = _arc(th0, ph0, tt, pp)
+    improved = (o[:, 0] > start) & (dist <= max_cells * spacing)
     return Refined(theta=np.where(improved, tt, th0), phi=np.where(improved, pp, ph0),
-                   statistic=np.where(improved, o[:, 0], grid_stat), grid_statistic=grid_stat,
-                   improved=improved, trace=trace)
+                   statistic=np.where(improved, o[:, 0], start), start_statistic=start,
+                   grid_statistic=np.asarray(grid_stat, np.float64), improved=improved,
+                   distance=np.where(improved, dist, 0.0), trace=trace)

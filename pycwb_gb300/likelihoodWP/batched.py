@@ -169,6 +169,7 @@ class BatchedSkyLoop:
     # -- steps -------------------------------------------------------------
     def upload(self):
         """Host (pinned) -> device copies of the cluster data, async on the stream."""
+        self.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(self.stream):
             self.td00.copy_(self.b.td00, non_blocking=True)
             self.td90.copy_(self.b.td90, non_blocking=True)
@@ -255,6 +256,26 @@ def sky_loop_batched(tables: SkyTables, clusters, shape=None):
     batch = clusters if isinstance(clusters, ClusterBatch) else ClusterBatch.from_clusters(clusters)
     loop = BatchedSkyLoop(tables, batch, shape=shape)
     return loop.run()
+
+
+def shard_clusters(sizes, world: int, rank: int) -> np.ndarray:
+    """Cluster indices of `rank` when clusters are spread over `world` GPUs.
+
+    Clusters are independent (likelihood.py:58-135), so ranks share no data;
+    the work of a cluster is proportional to its pixel count, and clusters
+    are dealt largest first to the least-loaded rank (LPT).  Every rank
+    computes the same assignment, so no communication is needed."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if world < 1 or not (0 <= rank < world):
+        raise ValueError("need world >= 1 and 0 <= rank < world")
+    order = np.argsort(-sizes, kind="stable")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.empty(sizes.size, dtype=np.int64)
+    for c in order:
+        r = int(np.argmin(load))
+        owner[c] = r
+        load[r] += max(int(sizes[c]), 1)
+    return np.flatnonzero(owner == rank)
 
 
 def n_work_items(n_valid: int, n_clusters: int, shape: _lib.TileShape | None) -> int:

@@ -77,7 +77,7 @@ def calculate_dpf(FP, FX, rms, n_sky, n_ifo, gamma_regulator, network_energy_thr
     n_sky, n_ifo = int(n_sky), int(n_ifo)
     _check_tables(FP, FX, rms, n_sky, n_ifo)
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     FPd, FXd = dv.to_device(FP, torch.float32), dv.to_device(FX, torch.float32)
     rmsd = dv.to_device(rms, torch.float32)
     valid = _valid(sky_valid_indices, n_sky)
@@ -92,6 +92,7 @@ def calculate_dpf(FP, FX, rms, n_sky, n_ifo, gamma_regulator, network_energy_thr
                              ws.data_ptr(), ws.numel(), dv.stream_handle(s))
     _lib.check(rc, "calculate_dpf")
     if return_device:
+        dv.end(s, out)
         return out
     with torch.cuda.stream(s):
         return float(out.item())
@@ -99,6 +100,7 @@ def calculate_dpf(FP, FX, rms, n_sky, n_ifo, gamma_regulator, network_energy_thr
 
 def _scan_outputs(stats, res, return_device, s):
     if return_device:
+        dv.end(s, stats, res)
         return stats, res
     with torch.cuda.stream(s):
         st = stats.cpu().numpy()
@@ -123,7 +125,7 @@ def scan_sky_for_best_fit(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG,
                          f"got td00: {dv.shape_of(td00)}, td90: {dv.shape_of(td90)}, "
                          f"rms: {dv.shape_of(rms)}")
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     FPd, FXd = dv.to_device(FP, torch.float32), dv.to_device(FX, torch.float32)
     rmsd = dv.to_device(rms, torch.float32)
     t0, t9 = dv.to_device(td00, torch.float32), dv.to_device(td90, torch.float32)
@@ -161,7 +163,7 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     if dv.shape_of(td00) != (n_delay, n_ifo, n_pix) or dv.shape_of(td90) != dv.shape_of(td00):
         raise ValueError("td00/td90 must have shape (n_delay, n_ifo, n_pix)")
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     FPd, FXd = dv.to_device(FP, torch.float32), dv.to_device(FX, torch.float32)
     rmsd = dv.to_device(rms, torch.float32)
     t0, t9 = dv.to_device(td00, torch.float32), dv.to_device(td90, torch.float32)
@@ -181,6 +183,7 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
                         ws.data_ptr(), ws.numel(), dv.stream_handle(s))
     _lib.check(rc, "sky_loop")
     if return_device:
+        dv.end(s, reg, stats, res)
         return reg, stats, res
     out = _scan_outputs(stats, res, False, s)
     with torch.cuda.stream(s):

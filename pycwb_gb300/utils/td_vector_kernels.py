@@ -30,7 +30,7 @@ def batch_get_td_vecs(pixel_indices, padded00, padded90, T0, Tx, M, n_coeffs, K,
     if dv.shape_of(T0) != (2 * J + 1, 2 * n_coeffs + 1) or dv.shape_of(Tx) != dv.shape_of(T0):
         raise ValueError(f"T0/Tx must be (2J+1, 2*n_coeffs+1) = ({2 * J + 1}, {2 * n_coeffs + 1})")
     L = _lib.load()
-    s = dv.stream()
+    s = dv.begin()
     idx = dv.to_device(pixel_indices, torch.int32)
     p00, p90 = dv.to_device(padded00, torch.float32), dv.to_device(padded90, torch.float32)
     t0, tx = dv.to_device(T0, torch.float64), dv.to_device(Tx, torch.float64)
@@ -43,6 +43,7 @@ def batch_get_td_vecs(pixel_indices, padded00, padded90, T0, Tx, M, n_coeffs, K,
                                  out.data_ptr(), dv.stream_handle(s))
     _lib.check(rc, "batch_get_td_vecs")
     if return_device:
+        dv.end(s, out)
         return out
     with torch.cuda.stream(s):
         return out.cpu().numpy()
