@@ -198,6 +198,23 @@ int pgw_batch_get_td_vecs(const int32_t* pixel_indices, int64_t n_pixels, const 
                           const double* phase, int M, int n_coeffs, int K, int J, float* out,
                           void* stream);
 
+/* td-amplitude vectors written straight into the batched scan's inputs: the
+ * amplitudes of pgw_batch_get_td_vecs for the n_pixels pixels of one
+ * (WDM plane, detector `ifo`) go to cluster dst_cluster[p], local pixel
+ * dst_pixel[p], of td00_all/td90_all laid out as in pgw_sky_loop_batched
+ * (pix_offsets, td_offsets, n_ifo).  Replaces, for the scan's purposes, the
+ * per-(layer, detector) calls of pycwb/modules/super_cluster_native/
+ * super_cluster.py:545-564 followed by the dense -> CSR -> (D, I, P)
+ * rearrangements of pixel_arrays.py:251-258 and likelihood.py:303-304.
+ * Destinations outside [0, n_clusters) x [0, P_c) are skipped. */
+int pgw_td_vecs_to_clusters(const int32_t* pixel_indices, int64_t n_pixels,
+                            const int32_t* dst_cluster, const int32_t* dst_pixel, int n_clusters,
+                            const int64_t* pix_offsets, const int64_t* td_offsets, int ifo,
+                            int n_ifo, const float* padded00, const float* padded90, int64_t rows,
+                            const double* T0, const double* Tx, const double* phase, int M,
+                            int n_coeffs, int K, int J, float* td00_all, float* td90_all,
+                            void* stream);
+
 /* Sky statistic at continuous directions and its gradient (no counterpart
  * in the reference, which evaluates the statistic only on the grid).  For
  * query q: cluster query_cluster[q] of the concatenated batch (layouts as in

@@ -99,6 +99,9 @@ def load():
         L.pgw_sky_loop_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
                                            f64, f64, f64, P, i64, P, P, P, P, P, P, sz, P]
         L.pgw_sky_order.argtypes = [P, i32, i64, P, i64, P, P]
+        L.pgw_td_vecs_to_clusters.argtypes = [P, i64, P, P, i32, P, P, i32, i32, P, P, i64, P, P, P, i32,
+                                              i32, i32, i32, P, P, P]
+        L.pgw_td_vecs_to_clusters.restype = ctypes.c_int
         L.pgw_sky_stat_grad.argtypes = [i32, i32, P, P, P, P, P, P, P, P, i32, P, f32, P, f64, P, P]
         L.pgw_sky_stat_grad.restype = ctypes.c_int
         L.pgw_refine_sky.argtypes = [i32, i32, P, P, P, P, P, P, P, P, i32, P, f32, P, f64, i32, f32,

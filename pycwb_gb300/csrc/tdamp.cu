@@ -117,7 +117,85 @@ __global__ void td_vecs_kernel(const int32_t* __restrict__ pixel_indices, int64_
   out[p * 2 * half + half + ki] = static_cast<float>(a90);
 }
 
+// Same amplitudes, written into the batched scan's cluster layout: pixel p
+// of this (plane, detector) belongs to cluster dst_cluster[p] at local
+// position dst_pixel[p]; a00(dT) goes to td00_all[td_off[c] + ((dT+K) *
+// n_ifo + ifo) * P_c + j], as the reference's set_td_amp_from_dense and the
+// transposes of likelihood.py:303-304 would arrange it.
+__global__ void td_vecs_scatter_kernel(const int32_t* __restrict__ pixel_indices, int64_t n_pixels,
+                                       const int32_t* __restrict__ dst_cluster,
+                                       const int32_t* __restrict__ dst_pixel, int n_clusters,
+                                       const int64_t* __restrict__ pix_offsets,
+                                       const int64_t* __restrict__ td_offsets, int ifo, int n_ifo,
+                                       const float* __restrict__ p00, const float* __restrict__ p90,
+                                       int64_t rows, const double* __restrict__ T0,
+                                       const double* __restrict__ Tx,
+                                       const double* __restrict__ phase, int M, int nc, int K,
+                                       int J, float* __restrict__ td00_all,
+                                       float* __restrict__ td90_all) {
+  const int half = 2 * K + 1;
+  const int64_t gid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= n_pixels * half) return;
+  const int64_t p = gid / half;
+  const int ki = static_cast<int>(gid % half);
+  const int64_t idx = pixel_indices[p];
+  const int64_t n = idx / (M + 1);
+  const int m = static_cast<int>(idx % (M + 1));
+  const int dT = ki - K;
+  const int shift = dT >= 0 ? dT / J : -((-dT) / J);
+  const int sub = dT - shift * J;
+  const int64_t ne = n - shift;
+  double a00, a90;
+  if (shift % 2 != 0) {
+    const double x = pixel_amplitude(ne, m, sub, p90, rows, T0, Tx, M, nc, J, true, phase);
+    const double y = pixel_amplitude(ne, m, sub, p00, rows, T0, Tx, M, nc, J, false, phase);
+    if ((n + m) % 2 != 0) { a00 = -x; a90 = y; } else { a00 = x; a90 = -y; }
+  } else {
+    a00 = pixel_amplitude(ne, m, sub, p00, rows, T0, Tx, M, nc, J, false, phase);
+    a90 = pixel_amplitude(ne, m, sub, p90, rows, T0, Tx, M, nc, J, true, phase);
+  }
+  const int c = dst_cluster[p];
+  if (c < 0 || c >= n_clusters) return;  // a bad destination is dropped, never written
+  const int64_t P = pix_offsets[c + 1] - pix_offsets[c];
+  const int64_t j = dst_pixel[p];
+  if (j < 0 || j >= P) return;
+  const int64_t o = td_offsets[c] + (static_cast<int64_t>(ki) * n_ifo + ifo) * P + j;
+  td00_all[o] = static_cast<float>(a00);
+  td90_all[o] = static_cast<float>(a90);
+}
+
 }  // namespace
+
+extern "C" int pgw_td_vecs_to_clusters(const int32_t* pixel_indices, int64_t n_pixels,
+                                       const int32_t* dst_cluster, const int32_t* dst_pixel,
+                                       int n_clusters, const int64_t* pix_offsets, const int64_t* td_offsets,
+                                       int ifo, int n_ifo, const float* padded00,
+                                       const float* padded90, int64_t rows, const double* T0,
+                                       const double* Tx, const double* phase, int M, int n_coeffs,
+                                       int K, int J, float* td00_all, float* td90_all,
+                                       void* stream) {
+  if (M < 1 || n_coeffs < 0 || K < 0 || J < 1 || rows < 0 || n_pixels < 0)
+    return pgw::fail(PGW_ERR_BAD_SHAPE, "td vectors need M >= 1, J >= 1, K >= 0, n_coeffs >= 0");
+  if (n_clusters < 0) return pgw::fail(PGW_ERR_BAD_SHAPE, "n_clusters must be >= 0");
+  if (ifo < 0 || ifo >= n_ifo || n_ifo > PGW_MAX_IFO)
+    return pgw::fail(PGW_ERR_BAD_SHAPE, "ifo must be in [0, n_ifo), n_ifo <= 8");
+  if (n_pixels == 0) return PGW_OK;
+  if (!pixel_indices || !dst_cluster || !dst_pixel || !pix_offsets || !td_offsets || !padded00 ||
+      !padded90 || !T0 || !Tx || !phase || !td00_all || !td90_all)
+    return pgw::fail(PGW_ERR_BAD_ARGUMENT, "NULL device pointer");
+  const int64_t total = n_pixels * (2 * K + 1);
+  const int threads = 256;
+  const int64_t blocks = (total + threads - 1) / threads;
+  if (blocks > 0x7fffffffLL) return pgw::fail(PGW_ERR_BAD_SHAPE, "too many pixels");
+  td_vecs_scatter_kernel<<<static_cast<unsigned>(blocks), threads, 0,
+                           static_cast<cudaStream_t>(stream)>>>(
+      pixel_indices, n_pixels, dst_cluster, dst_pixel, n_clusters, pix_offsets, td_offsets, ifo, n_ifo,
+      padded00, padded90, rows, T0, Tx, phase, M, n_coeffs, K, J, td00_all, td90_all);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return pgw::fail(PGW_ERR_CUDA, std::string("td_vecs_scatter_kernel: ") + cudaGetErrorString(e));
+  return PGW_OK;
+}
 
 extern "C" int pgw_batch_get_td_vecs(const int32_t* pixel_indices, int64_t n_pixels,
                                      const float* padded00, const float* padded90, int64_t rows,

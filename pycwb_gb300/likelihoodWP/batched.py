@@ -167,12 +167,15 @@ class BatchedSkyLoop:
         self.graph = None
 
     # -- steps -------------------------------------------------------------
-    def upload(self):
-        """Host (pinned) -> device copies of the cluster data, async on the stream."""
+    def upload(self, *, td=True):
+        """Host (pinned) -> device copies of the cluster data, async on the stream.
+        td=False copies the rms only, for batches whose td amplitudes were
+        built on the device (utils.td_vector_kernels.td_vecs_to_clusters)."""
         self.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(self.stream):
-            self.td00.copy_(self.b.td00, non_blocking=True)
-            self.td90.copy_(self.b.td90, non_blocking=True)
+            if td:
+                self.td00.copy_(self.b.td00, non_blocking=True)
+                self.td90.copy_(self.b.td90, non_blocking=True)
             self.rms.copy_(self.b.rms, non_blocking=True)
 
     def launch(self):

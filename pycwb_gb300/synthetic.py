@@ -139,3 +139,91 @@ def make_batch_device(seed, sizes, ml, FP_t, FX_t, K, snr_lo=8.0, snr_hi=40.0, s
             td00.index_add_(0, idx, (prof[:, i] * s00[:, i]).to(torch.float32))
             td90.index_add_(0, idx, (prof[:, i] * s90[:, i]).to(torch.float32))
     return td00, td90, rms, l_true, snr
+
+
+def make_lag(seed, ifos, ml, FP_t, FX_t, *, layers=(16, 32, 64, 128, 256, 512), duration=600.0,
+             rate_ana=512, up_tdf=4, n_coeffs=12, n_clusters=1024, size_lo=50, size_hi=5000,
+             snr_lo=8.0, snr_hi=40.0, device="cuda"):
+    """A synthetic lag for LagPipeline: WDM planes, TD filters and clusters.
+
+    Per resolution M (M+1 layers over duration * rate_ana samples) and
+    detector, padded 00/90 planes of unit-variance Gaussian noise (on the
+    device) and TD filters T0/Tx of shape (2J+1, 2*n_coeffs+1), J = M * up_tdf:
+    T0 carries a unit centre tap tapered with the delay plus small random
+    taps, Tx small random taps.  The filters are not the WDM basis's (the
+    WDM library is not available offline); they give td amplitudes of the
+    right shapes, magnitudes and cost.  Each cluster picks a resolution and
+    P ~ log-uniform[size_lo, size_hi] distinct pixels in a compact
+    time-frequency box; its pixels carry a coherent signal of network SNR
+    ~ U[snr_lo, snr_hi] from a random direction (F+/Fx weighted as in
+    make_cluster), added to every detector's planes.
+    Returns (planes, cluster_level, cluster_pixels, rms, l_true)."""
+    import torch
+
+    from .types.td_batch_inputs import TDBatchInputs
+
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    n_ifo = len(ifos)
+    n_sky = ml.shape[1]
+    nc = int(n_coeffs)
+    planes, shapes = {}, {}
+    for M in layers:
+        M = int(M)
+        n_time = int(duration * rate_ana) // M
+        rows = n_time + 2 * nc
+        J = M * int(up_tdf)
+        d = np.arange(-J, J + 1, dtype=np.float64)
+        per = []
+        for _ in range(n_ifo):
+            p00 = torch.zeros((rows, M + 1), dtype=torch.float32, device=device)
+            p90 = torch.zeros_like(p00)
+            p00[nc:nc + n_time] = torch.randn((n_time, M + 1), generator=g, device=device)
+            p90[nc:nc + n_time] = torch.randn((n_time, M + 1), generator=g, device=device)
+            T0 = rng.standard_normal((2 * J + 1, 2 * nc + 1)) * (0.05 / math.sqrt(2 * nc + 1))
+            T0[:, nc] += np.cos(0.5 * math.pi * d / J)
+            Tx = rng.standard_normal((2 * J + 1, 2 * nc + 1)) * (0.1 / math.sqrt(2 * nc + 1))
+            per.append(TDBatchInputs(p00, p90, torch.from_numpy(T0).to(device),
+                                     torch.from_numpy(Tx).to(device), M, nc, J))
+        planes[M] = per
+        shapes[M] = (n_time, M + 1)
+
+    sizes = log_uniform_sizes(rng, n_clusters, size_lo, size_hi)
+    level = rng.choice(np.asarray(layers, np.int64), size=n_clusters)
+    pixels, rms, l_true = [], [], rng.integers(n_sky, size=n_clusters)
+    for c in range(n_clusters):
+        M = int(level[c])
+        n_time, n_f = shapes[M]
+        P = int(min(sizes[c], n_time * n_f // 2))
+        wf = int(min(n_f, max(1, math.ceil(math.sqrt(2 * P)))))
+        wt = int(min(n_time, math.ceil(2 * P / wf)))
+        n0 = int(rng.integers(0, n_time - wt + 1))
+        m0 = int(rng.integers(0, n_f - wf + 1))
+        box = rng.choice(wt * wf, size=P, replace=False)
+        n, m = n0 + box // wf, m0 + box % wf
+        idx = (n * n_f + m).astype(np.int32)
+        pixels.append(idx)
+        r = make_rms(rng, P, n_ifo)
+        rms.append(r)
+        w = np.exp(rng.standard_normal(P))
+        w /= w.sum()
+        h = rng.standard_normal((4, P)) * np.sqrt(w)[None, :]
+        fp = FP_t[l_true[c]].astype(np.float64)
+        fx = FX_t[l_true[c]].astype(np.float64)
+        rr = r.astype(np.float64)
+        s00 = rr * (fp[None, :] * h[0][:, None] + fx[None, :] * h[1][:, None])
+        s90 = rr * (fp[None, :] * h[2][:, None] + fx[None, :] * h[3][:, None])
+        e = float(np.sum(s00 ** 2 + s90 ** 2))
+        if e > 0.0:
+            k = rng.uniform(snr_lo, snr_hi) / math.sqrt(e)
+            s00 *= k
+            s90 *= k
+        rows_t = torch.from_numpy((n + nc).astype(np.int64)).to(device)
+        cols_t = torch.from_numpy(m.astype(np.int64)).to(device)
+        for i, t in enumerate(planes[M]):
+            t.padded00.index_put_((rows_t, cols_t), torch.from_numpy(
+                s00[:, i].astype(np.float32)).to(device), accumulate=True)
+            t.padded90.index_put_((rows_t, cols_t), torch.from_numpy(
+                s90[:, i].astype(np.float32)).to(device), accumulate=True)
+    return planes, level, pixels, rms, l_true

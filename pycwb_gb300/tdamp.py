@@ -44,3 +44,21 @@ def td_phase_table(M: int, J: int) -> np.ndarray:
     if M < 1 or J < 1:
         raise ValueError(f"td phase table needs M >= 1 and J >= 1, got M={M}, J={J}")
     return np.frombuffer(_phase_table_cached(M, J), dtype=np.float64).reshape(M + 1, 2 * J + 1, 4)
+
+
+_device_tables: dict = {}
+
+
+def td_phase_table_device(M: int, J: int, device):
+    """td_phase_table(M, J) as a float64 CUDA tensor, copied to `device` once
+    and kept (the largest, M = 512 and J = 2048, is 67 MB)."""
+    import torch
+
+    dev = torch.device(device)
+    key = (int(M), int(J), dev.index if dev.index is not None else torch.cuda.current_device())
+    t = _device_tables.get(key)
+    if t is None:
+        t = torch.from_numpy(td_phase_table(M, J).copy()).to(torch.device("cuda", key[2]))
+        torch.cuda.synchronize(key[2])   # complete before any stream reads it
+        _device_tables[key] = t
+    return t
