@@ -372,6 +372,19 @@ def main():
     achieved = useful_ops / (kernel_ms * 1e-3) / 1e12
     traffic = traffic_from_profile(args.clusters, total_pix)
 
+    # ---- the regulator alone (pgw_calculate_dpf_batched), same device data --
+    with torch.cuda.stream(loop.stream):
+        reg_buf = torch.empty(args.clusters, dtype=torch.float64, device=dev)
+    loop.launch_regulators(reg_buf)
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    r0.record(loop.stream)
+    loop.launch_regulators(reg_buf)
+    r1.record(loop.stream)
+    r1.synchronize()
+    reg_only_ms = r0.elapsed_time(r1)
+    assert np.array_equal(reg_buf.cpu().numpy(), res.regulator)
+
     # ---- end to end through the public API ------------------------------
     e2e = None
     if not args.no_e2e:
@@ -440,6 +453,7 @@ def main():
             "clocks": clk,
             "plain": plain,
             "batched_vs_plain": (plain["ms"] / ms_per_step) if plain else None,
+            "regulator_only_ms": reg_only_ms,
             "adjoint": adjoint,
             "td_build": td_build,
             "pipeline": pipeline,
@@ -458,6 +472,33 @@ def ctypes_peak(L):
     rc = L.pgw_fp32_fma_peak(20000, ctypes.byref(out), ctypes.byref(ms),
                              torch.cuda.current_stream().cuda_stream)
     return out.value if rc == 0 else None
+
+
+def fp64_peak(L):
+    """Measured float64 multiply + add rate (G ops/s) of this GPU."""
+    import ctypes
+    import torch
+    out = ctypes.c_double(0.0)
+    ms = ctypes.c_double(0.0)
+    rc = L.pgw_fp64_mul_add_peak(400, ctypes.byref(out), ctypes.byref(ms),
+                                 torch.cuda.current_stream().cuda_stream)
+    return out.value if rc == 0 else None
+
+
+def td_ops(taps: int) -> int:
+    """float64 multiplies + adds of one (pixel, delay) td pair at an interior
+    layer: two amplitudes, each three FIRs of `taps` products and sums plus
+    nine to combine them with the phase factors (td_vector_kernels.py:40-131)."""
+    return 2 * (6 * taps + 9)
+
+
+def td_roofline(L, pairs: int, taps: int, ms: float):
+    peak = fp64_peak(L)
+    achieved = pairs * td_ops(taps) / (ms * 1e-3) / 1e9
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "G ops/s",
+            "frac": achieved / peak if peak else None, "ops_per_pair": td_ops(taps),
+            "peak_source": "measured: pgw_fp64_mul_add_peak (separately rounded multiply and "
+                           "add chains) in this run"}
 
 
 def traffic_from_profile(n_clusters, total_pix):
@@ -531,8 +572,10 @@ def time_td_build(dev, n_pix=1_000_000, M=64, nc=20, K=20):
     e1.record(s)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
+    from pycwb_gb300 import _lib
     return {"pixels": n_pix, "layers": M, "K": K, "taps": 2 * nc + 1, "ms": ms,
             "pixels_per_s": n_pix / (ms * 1e-3),
+            "roofline": td_roofline(_lib.load(), n_pix * (2 * K + 1), 2 * nc + 1, ms),
             "note": "float64 accumulation, bit-identical to the reference"}
 
 
@@ -548,7 +591,7 @@ def time_pipeline(dev, seed, n_clusters=1024, steps=2):
     regulator + scan over HEALPix 8, refinement of every sky maximum."""
     import torch
 
-    from pycwb_gb300 import sky
+    from pycwb_gb300 import _lib, sky
     from pycwb_gb300.adjoint import detector_geometry
     from pycwb_gb300.likelihoodWP.batched import SkyTables
     from pycwb_gb300.likelihoodWP.lag_pipeline import LagPipeline
@@ -591,6 +634,8 @@ def time_pipeline(dev, seed, n_clusters=1024, steps=2):
         "steps": steps, "ms_per_lag": wall * 1e3, **st,
         "cluster_sky_evals_per_s": n_clusters * n_sky / (wall),
         "scan_cluster_sky_evals_per_s": n_clusters * n_sky / (st["sky_loop_ms"] * 1e-3),
+        "td_roofline": td_roofline(_lib.load(), pipe.total_pix * len(PIPE_IFOS) * (2 * PIPE_K + 1),
+                                   25, st["td_build_ms"]),
         "h2d_bytes_per_lag": pipe.h2d_bytes, "found": int(out.scan.found.sum()),
         "refined": int(r.improved.sum()) if r is not None else 0,
         "setup_s": round(t_set, 2),

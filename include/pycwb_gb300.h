@@ -185,6 +185,21 @@ int pgw_sky_loop_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                          const pgw_tile_shape* shape, void* workspace, size_t workspace_bytes,
                          void* stream);
 
+/* Regulator only, for every cluster of a batch in one launch: REG[1] of each
+ * cluster (pgw_calculate_dpf's value) into out_regulators[n_clusters]
+ * (float64).  The batched form of pycwb/modules/likelihoodWP/dpf.py:8-34 as
+ * likelihood.py:310-312 calls it per cluster; rms_all and pix_offsets as in
+ * pgw_sky_loop_batched, workspace of pgw_workspace_bytes(n_ifo, 1, total_pix,
+ * n_clusters) bytes.  sky_order (optional) is the order the directions are
+ * visited in, which does not change the result. */
+int pgw_calculate_dpf_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
+                              int64_t total_pix, int64_t n_sky, const float* FP, const float* FX,
+                              const float* rms_all, double gamma_regulator,
+                              double network_energy_threshold, const int64_t* sky_valid_indices,
+                              int64_t n_valid, const int32_t* sky_order, double* out_regulators,
+                              const pgw_tile_shape* shape, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
 /* td-amplitude vectors of n_pixels pixels of one (layer, detector) plane:
  * out (n_pixels, 4K+2) float32 = [a00(-K..K), a90(-K..K)] per pixel.
  * Replaces batch_get_td_vecs, pycwb/utils/td_vector_kernels.py:133-199
@@ -252,6 +267,11 @@ int pgw_refine_sky(int n_ifo, int n_queries, const int32_t* query_cluster, const
  * timed launch of `iters` x 128 register FMAs per thread; the sky loop's
  * FP32 roofline is reported against this number.  Synchronous. */
 int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* stream);
+
+/* Measured float64 multiply + add throughput (G ops/s, a multiply and an add
+ * counted as one op each, issued as separate correctly rounded instructions):
+ * the denominator of the td-amplitude build's roofline.  Synchronous. */
+int pgw_fp64_mul_add_peak(int iters, double* out_gops, double* out_ms, void* stream);
 
 #ifdef __cplusplus
 }

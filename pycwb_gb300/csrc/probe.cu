@@ -1,7 +1,8 @@
-// FP32 FMA throughput probe: the measured denominator of the sky loop's
-// FP32 roofline.  Every thread runs 8 independent chains of fused
-// multiply-adds on registers (no memory traffic inside the loop); the host
-// times the launch with CUDA events.
+// Arithmetic throughput probes, the measured denominators of the rooflines:
+// FP32 FMA (the sky loop) and float64 multiply/add issued as separate,
+// separately rounded instructions (the td-amplitude build).  Every thread
+// runs 8 independent register chains (no memory traffic inside the loop);
+// the host times the launch with CUDA events.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -28,30 +29,73 @@ __global__ void __launch_bounds__(256) fma_chains_kernel(int iters, float a, flo
   if (s == 12345.678f) sink[threadIdx.x] = s;  // keeps the chains alive
 }
 
-}  // namespace
+// Chains of __dmul_rn then __dadd_rn: one multiply and one add per step, the
+// instruction mix of td_vecs_kernel's FIRs.
+__global__ void __launch_bounds__(256) dmul_dadd_chains_kernel(int iters, double a, double b,
+                                                               double* sink) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k * 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) x[k] = __dadd_rn(__dmul_rn(x[k], a), b);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678) sink[threadIdx.x] = s;
+}
 
-extern "C" int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* stream) {
-  if (iters < 1 || !out_tflops) return pgw::fail(PGW_ERR_BAD_ARGUMENT, "iters >= 1 and an output");
+template <typename Kernel, typename T>
+int time_probe(Kernel kernel, int iters, T a, T b, void* stream, int* n_sm_out, float* ms_out) {
   int dev = 0, n_sm = 0;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return pgw::fail(PGW_ERR_CUDA, "device query failed");
-  const int blocks = n_sm * 8, threads = 256;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  fma_chains_kernel<<<blocks, threads, 0, s>>>(iters / 4 + 1, 0.999999f, 1e-7f, nullptr);  // warm-up
+  kernel<<<n_sm * 8, 256, 0, s>>>(iters / 4 + 1, a, b, nullptr);  // warm-up
   cudaEventRecord(e0, s);
-  fma_chains_kernel<<<blocks, threads, 0, s>>>(iters, 0.999999f, 1e-7f, nullptr);
+  kernel<<<n_sm * 8, 256, 0, s>>>(iters, a, b, nullptr);
   cudaEventRecord(e1, s);
   const cudaError_t e = cudaEventSynchronize(e1);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (e != cudaSuccess) return pgw::fail(PGW_ERR_CUDA, std::string("fma probe: ") + cudaGetErrorString(e));
-  const double fmas = static_cast<double>(blocks) * threads * iters * 16.0 * 8.0;
+  if (e != cudaSuccess) return pgw::fail(PGW_ERR_CUDA, std::string("probe: ") + cudaGetErrorString(e));
+  if (ms <= 0.f) return pgw::fail(PGW_ERR_CUDA, "probe: no elapsed time");
+  *n_sm_out = n_sm;
+  *ms_out = ms;
+  return PGW_OK;
+}
+
+}  // namespace
+
+extern "C" int pgw_fp64_mul_add_peak(int iters, double* out_gops, double* out_ms, void* stream) {
+  if (iters < 1 || !out_gops) return pgw::fail(PGW_ERR_BAD_ARGUMENT, "iters >= 1 and an output");
+  int n_sm = 0;
+  float ms = 0.f;
+  const int rc = time_probe(dmul_dadd_chains_kernel, iters, 0.999999999, 1e-9, stream, &n_sm, &ms);
+  if (rc != PGW_OK) return rc;
+  const double ops = 2.0 * n_sm * 8.0 * 256.0 * iters * 8.0 * 8.0;  // one mul + one add per step
+  *out_gops = ops / (ms * 1e-3) / 1e9;
+  if (out_ms) *out_ms = ms;
+  return PGW_OK;
+}
+
+extern "C" int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* stream) {
+  if (iters < 1 || !out_tflops) return pgw::fail(PGW_ERR_BAD_ARGUMENT, "iters >= 1 and an output");
+  int n_sm = 0;
+  float ms = 0.f;
+  const int rc = time_probe(fma_chains_kernel, iters, 0.999999f, 1e-7f, stream, &n_sm, &ms);
+  if (rc != PGW_OK) return rc;
+  const double fmas = static_cast<double>(n_sm) * 8 * 256 * iters * 16.0 * 8.0;
   *out_tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
   if (out_ms) *out_ms = ms;
   return PGW_OK;

@@ -190,6 +190,27 @@ class BatchedSkyLoop:
             self.ws.numel(), self.stream.cuda_stream)
         _lib.check(rc, "sky_loop_batched")
 
+    def launch_regulators(self, out: torch.Tensor):
+        """Regulator only for every cluster (pgw_calculate_dpf_batched) into
+        `out` (n_clusters float64, device), on the loop's stream; the rms must
+        be on the device (upload)."""
+        t, b = self.t, self.b
+        rc = self.L.pgw_calculate_dpf_batched(
+            b.n_ifo, b.n_clusters, self.pix_off.data_ptr(), b.total_pix, t.n_sky,
+            t.FP.data_ptr(), t.FX.data_ptr(), self.rms.data_ptr(), t.gamma_regulator,
+            t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(), t.order.data_ptr(),
+            out.data_ptr(), None if self.shape is None else ctypes.byref(self.shape),
+            self.ws.data_ptr(), self.ws.numel(), self.stream.cuda_stream)
+        _lib.check(rc, "calculate_dpf_batched")
+
+    def regulators(self) -> np.ndarray:
+        """REG[1] of every cluster (float64), regulator only."""
+        with torch.cuda.stream(self.stream):
+            out = torch.empty(self.b.n_clusters, dtype=torch.float64, device=self.regs.device)
+        self.launch_regulators(out)
+        with torch.cuda.stream(self.stream):
+            return out.cpu().numpy()
+
     def download(self):
         """Device -> host (pinned) copies of the per-cluster results, async."""
         with torch.cuda.stream(self.stream):

@@ -105,3 +105,22 @@ def test_batched_graph_replay_is_repeatable(env):
         np.testing.assert_array_equal(first.sky_stat_max, again.sky_stat_max)
         np.testing.assert_array_equal(first.regulator, again.regulator)
         assert bool((loop.stats == maps0).all())
+
+
+def test_batched_regulators_only(env, oracle_mod):
+    """pgw_calculate_dpf_batched gives the full loop's REG[1], bit for bit,
+    and the oracle's regulator for every cluster."""
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch
+
+    clusters = _clusters(env, [3, 250, 0, 1200, 64], seed=21)
+    loop = BatchedSkyLoop(env["tables"], ClusterBatch.from_clusters(clusters))
+    full = loop.run()
+    only = loop.regulators()
+    assert np.array_equal(only, full.regulator)
+    reg, FP_t, FX_t = env["reg"], env["FP_t"], env["FX_t"]
+    n_sky = FP_t.shape[0]
+    valid = np.arange(n_sky, dtype=np.int64)
+    for c, (_, _, rms) in enumerate(clusters):
+        ref = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
+                                       reg["network_energy_threshold"], valid)
+        assert np.float32(only[c]) == np.float32(ref), c
