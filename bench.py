@@ -670,7 +670,7 @@ def time_plain(L, loop, tables, batch, shape, dev):
                             t0, t9, batch.n_delay, tables.ml.data_ptr(), tables.REG0,
                             tables.gamma_regulator, tables.netCC, tables.network_energy_threshold,
                             tables.valid.data_ptr(), tables.valid.numel(), tables.order.data_ptr(),
-                            st.data_ptr(),
+                            tables.reg_order.data_ptr(), st.data_ptr(),
                             res.data_ptr() + 32 * c, regs.data_ptr() + 8 * c, shp, ws.data_ptr(),
                             ws.numel(), s.cuda_stream)
         if rc:

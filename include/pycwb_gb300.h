@@ -79,6 +79,19 @@ size_t pgw_workspace_bytes(int n_ifo, int n_delay, int64_t total_pix, int n_clus
 int pgw_sky_order(const int32_t* ml, int n_ifo, int64_t n_sky, const int64_t* sky_valid_indices,
                   int64_t n_valid, int32_t* out_order, int64_t* out_n_tuples);
 
+/* Regulator order of the valid directions (host arrays, once per segment):
+ * out_order[0..n_valid) = positions of sky_valid_indices sorted by the mean,
+ * over fixed draws of normalised detector weights, of the regulator's
+ * per-pixel term fx / ni (FP, FX: (n_sky, n_ifo) float32).  The regulator
+ * decides most directions after part of the pixels (a running sum already
+ * over the threshold, or a bound on the rest already under it); the point
+ * depends mainly on that term, so this order gives the 32 directions of a
+ * warp similar stopping points.  Passed as `reg_order` to the sky-loop
+ * calls; results do not depend on it.  Counterpart of nothing in the
+ * reference (an execution order, not a result). */
+int pgw_regulator_order(const float* FP, const float* FX, int n_ifo, int64_t n_sky,
+                        const int64_t* sky_valid_indices, int64_t n_valid, int32_t* out_order);
+
 /* DPF regulator: REG[1] = (n_valid^2 / (n_pass^2 + 1e-9) - 1) * E_thr, where
  * n_pass counts valid directions whose DPF quality sqrt(NI / (NN + 0.01))
  * exceeds gamma_regulator.
@@ -128,13 +141,14 @@ typedef struct {
 /* Both passes for one cluster in one launch: the regulator, then the scan
  * with REG = {REG0, regulator, 0}.  Replaces the two calls at
  * pycwb/modules/likelihoodWP/likelihood.py:310-325 ("plain" path).  shape
- * may be NULL. */
+ * may be NULL.  reg_order: device int32 array from pgw_regulator_order, or
+ * NULL (the regulator then follows sky_order). */
 int pgw_sky_loop(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP, const float* FX,
                  const float* rms, const float* td00, const float* td90, int n_delay,
                  const int32_t* ml, float REG0, double gamma_regulator, double netCC,
                  double network_energy_threshold, const int64_t* sky_valid_indices,
-                 int64_t n_valid, const int32_t* sky_order, float* out_stats,
-                 pgw_scan_result* out_result, double* out_regulator,
+                 int64_t n_valid, const int32_t* sky_order, const int32_t* reg_order,
+                 float* out_stats, pgw_scan_result* out_result, double* out_regulator,
                  const pgw_tile_shape* shape, void* workspace, size_t workspace_bytes,
                  void* stream);
 
@@ -180,8 +194,8 @@ int pgw_sky_loop_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                          const float* td00_all, const float* td90_all, int n_delay,
                          const int32_t* ml, float REG0, double gamma_regulator, double netCC,
                          double network_energy_threshold, const int64_t* sky_valid_indices,
-                         int64_t n_valid, const int32_t* sky_order, float* out_stats,
-                         pgw_scan_result* out_results, double* out_regulators,
+                         int64_t n_valid, const int32_t* sky_order, const int32_t* reg_order,
+                         float* out_stats, pgw_scan_result* out_results, double* out_regulators,
                          const pgw_tile_shape* shape, void* workspace, size_t workspace_bytes,
                          void* stream);
 
@@ -190,13 +204,15 @@ int pgw_sky_loop_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
  * (float64).  The batched form of pycwb/modules/likelihoodWP/dpf.py:8-34 as
  * likelihood.py:310-312 calls it per cluster; rms_all and pix_offsets as in
  * pgw_sky_loop_batched, workspace of pgw_workspace_bytes(n_ifo, 1, total_pix,
- * n_clusters) bytes.  sky_order (optional) is the order the directions are
- * visited in, which does not change the result. */
+ * n_clusters) bytes.  sky_order and reg_order (optional, as in pgw_sky_loop)
+ * set the order the directions are visited in, which does not change the
+ * result. */
 int pgw_calculate_dpf_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                               int64_t total_pix, int64_t n_sky, const float* FP, const float* FX,
                               const float* rms_all, double gamma_regulator,
                               double network_energy_threshold, const int64_t* sky_valid_indices,
-                              int64_t n_valid, const int32_t* sky_order, double* out_regulators,
+                              int64_t n_valid, const int32_t* sky_order,
+                              const int32_t* reg_order, double* out_regulators,
                               const pgw_tile_shape* shape, void* workspace,
                               size_t workspace_bytes, void* stream);
 

@@ -95,10 +95,12 @@ def load():
         L.pgw_scan_sky_for_best_fit.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, P, f64, f64,
                                                 f64, P, i64, P, P, P, P, sz, P]
         L.pgw_sky_loop.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64, f64, P,
-                                   i64, P, P, P, P, P, P, sz, P]
+                                   i64, P, P, P, P, P, P, P, sz, P]
         L.pgw_sky_loop_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
-                                           f64, f64, f64, P, i64, P, P, P, P, P, P, sz, P]
+                                           f64, f64, f64, P, i64, P, P, P, P, P, P, P, sz, P]
         L.pgw_sky_order.argtypes = [P, i32, i64, P, i64, P, P]
+        L.pgw_regulator_order.argtypes = [P, P, i32, i64, P, i64, P]
+        L.pgw_regulator_order.restype = ctypes.c_int
         L.pgw_td_vecs_to_clusters.argtypes = [P, i64, P, P, i32, P, P, i32, i32, P, P, i64, P, P, P, i32,
                                               i32, i32, i32, P, P, P]
         L.pgw_td_vecs_to_clusters.restype = ctypes.c_int
@@ -111,7 +113,7 @@ def load():
         L.pgw_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, P, i32, i32, i32, i32, P, P]
         L.pgw_fp32_fma_peak.argtypes = [i32, P, P, P]
         L.pgw_calculate_dpf_batched.argtypes = [i32, i32, P, i64, i64, P, P, P, f64, f64, P, i64,
-                                                P, P, P, P, sz, P]
+                                                P, P, P, P, P, sz, P]
         L.pgw_calculate_dpf_batched.restype = ctypes.c_int
         L.pgw_fp64_mul_add_peak.argtypes = [i32, P, P, P]
         L.pgw_fp64_mul_add_peak.restype = ctypes.c_int
@@ -148,6 +150,22 @@ def sky_order(ml, sky_valid_indices):
                               valid.size, out.ctypes.data, ctypes.byref(n_t))
     check(rc, "sky_order")
     return out, int(n_t.value)
+
+
+def regulator_order(FP_t, FX_t, sky_valid_indices):
+    """Regulator order of the valid directions (host int32), pgw_regulator_order."""
+    import numpy as np
+    FP_t = np.ascontiguousarray(FP_t, dtype=np.float32)
+    FX_t = np.ascontiguousarray(FX_t, dtype=np.float32)
+    valid = np.ascontiguousarray(sky_valid_indices, dtype=np.int64)
+    if FP_t.ndim != 2 or FX_t.shape != FP_t.shape:
+        raise ValueError("FP/FX must both be (n_sky, n_ifo)")
+    out = np.empty(valid.size, dtype=np.int32)
+    rc = load().pgw_regulator_order(FP_t.ctypes.data, FX_t.ctypes.data, FP_t.shape[1],
+                                    FP_t.shape[0], valid.ctypes.data, valid.size,
+                                    out.ctypes.data)
+    check(rc, "regulator_order")
+    return out
 
 
 STATUS_NAMES = {

@@ -38,6 +38,7 @@ class SkyTables:
     ml: torch.Tensor
     valid: torch.Tensor
     order: torch.Tensor          # scan order of valid positions grouped by delay tuple
+    reg_order: torch.Tensor      # regulator order of valid positions (pgw_regulator_order)
     n_tuples: int
     n_ifo: int
     n_sky: int
@@ -58,10 +59,13 @@ class SkyTables:
         v_h = (sky_valid_indices.cpu().numpy() if isinstance(sky_valid_indices, torch.Tensor)
                else np.asarray(sky_valid_indices))
         order, n_tuples = _lib.sky_order(ml_h, v_h)
+        host = (lambda x: x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x))
+        reg_order = _lib.regulator_order(host(FP_t), host(FX_t), v_h)
         return cls(FP=dv.to_device(FP_t, torch.float32), FX=dv.to_device(FX_t, torch.float32),
                    ml=dv.to_device(ml, torch.int32),
                    valid=dv.to_device(sky_valid_indices, torch.int64),
-                   order=dv.to_device(order, torch.int32), n_tuples=int(n_tuples),
+                   order=dv.to_device(order, torch.int32),
+                   reg_order=dv.to_device(reg_order, torch.int32), n_tuples=int(n_tuples),
                    n_ifo=int(n_ifo),
                    n_sky=int(n_sky), network_energy_threshold=float(network_energy_threshold),
                    gamma_regulator=float(gamma_regulator), delta_regulator=float(delta_regulator),
@@ -185,7 +189,7 @@ class BatchedSkyLoop:
             t.n_sky, t.FP.data_ptr(), t.FX.data_ptr(), self.rms.data_ptr(), self.td00.data_ptr(),
             self.td90.data_ptr(), b.n_delay, t.ml.data_ptr(), t.REG0, t.gamma_regulator, t.netCC,
             t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(), t.order.data_ptr(),
-            self.stats.data_ptr(), self.res.data_ptr(), self.regs.data_ptr(),
+            t.reg_order.data_ptr(), self.stats.data_ptr(), self.res.data_ptr(), self.regs.data_ptr(),
             None if self.shape is None else ctypes.byref(self.shape), self.ws.data_ptr(),
             self.ws.numel(), self.stream.cuda_stream)
         _lib.check(rc, "sky_loop_batched")
@@ -199,7 +203,7 @@ class BatchedSkyLoop:
             b.n_ifo, b.n_clusters, self.pix_off.data_ptr(), b.total_pix, t.n_sky,
             t.FP.data_ptr(), t.FX.data_ptr(), self.rms.data_ptr(), t.gamma_regulator,
             t.network_energy_threshold, t.valid.data_ptr(), t.valid.numel(), t.order.data_ptr(),
-            out.data_ptr(), None if self.shape is None else ctypes.byref(self.shape),
+            t.reg_order.data_ptr(), out.data_ptr(), None if self.shape is None else ctypes.byref(self.shape),
             self.ws.data_ptr(), self.ws.numel(), self.stream.cuda_stream)
         _lib.check(rc, "calculate_dpf_batched")
 

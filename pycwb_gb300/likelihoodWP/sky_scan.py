@@ -64,6 +64,30 @@ def _sky_order_device(ml, sky_valid_indices, device):
     return t
 
 
+_reg_order_cache = {}
+
+
+def _reg_order_device(FP, FX, sky_valid_indices, device):
+    """Regulator order (pgw_regulator_order), cached per (FP, FX, valid)
+    like the scan order: it orders work only, never changes a result."""
+    def ident(x):
+        if isinstance(x, torch.Tensor):
+            return ("t", x.data_ptr(), tuple(x.shape))
+        a = np.asarray(x)
+        return ("n", id(x), a.__array_interface__["data"][0], a.shape)
+    key = (ident(FP), ident(FX), ident(sky_valid_indices))
+    hit = _reg_order_cache.get(key)
+    if hit is not None:
+        return hit
+    host = (lambda x: x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x))
+    order = _lib.regulator_order(host(FP), host(FX), host(sky_valid_indices))
+    t = torch.from_numpy(order).to(device)
+    if len(_reg_order_cache) > 16:
+        _reg_order_cache.clear()
+    _reg_order_cache[key] = t
+    return t
+
+
 def _valid(sky_valid_indices, n_sky):
     v = dv.to_device(sky_valid_indices, torch.int64)
     if v.ndim != 1 or v.numel() == 0:
@@ -170,6 +194,7 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     mld = dv.to_device(ml, torch.int32)
     valid = _valid(sky_valid_indices, n_sky)
     order = _sky_order_device(ml, sky_valid_indices, FPd.device) if sky_order else None
+    rorder = _reg_order_device(FP, FX, sky_valid_indices, FPd.device) if sky_order else None
     ws = dv.workspace(L.pgw_workspace_bytes(n_ifo, n_delay, n_pix, 1))
     with torch.cuda.stream(s):
         stats = torch.empty((N_STATS, n_sky), dtype=torch.float32, device=FPd.device)
@@ -178,7 +203,8 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     rc = L.pgw_sky_loop(n_ifo, n_pix, n_sky, FPd.data_ptr(), FXd.data_ptr(), rmsd.data_ptr(),
                         t0.data_ptr(), t9.data_ptr(), n_delay, mld.data_ptr(), float(np.float32(REG0)),
                         float(gamma_regulator), float(netCC), float(network_energy_threshold),
-                        valid.data_ptr(), valid.numel(), dv.ptr(order), stats.data_ptr(), res.data_ptr(),
+                        valid.data_ptr(), valid.numel(), dv.ptr(order), dv.ptr(rorder),
+                        stats.data_ptr(), res.data_ptr(),
                         reg.data_ptr(), None if shape is None else ctypes.byref(shape),
                         ws.data_ptr(), ws.numel(), dv.stream_handle(s))
     _lib.check(rc, "sky_loop")

@@ -47,3 +47,24 @@ def test_workspace_size_is_pure_host_arithmetic():
     assert a > 1000 * 252 * 4 and b > a
     assert L.pgw_workspace_bytes(0, 41, 10, 1) == 0
     assert L.pgw_workspace_bytes(9, 41, 10, 1) == 0
+
+
+def test_regulator_order_is_a_permutation():
+    """pgw_regulator_order runs on the host: a deterministic permutation of
+    the valid positions, and out-of-range sky indices are rejected."""
+    import numpy as np
+    from pycwb_gb300 import _lib, sky
+    try:
+        _lib.build()
+    except (RuntimeError, FileNotFoundError) as e:
+        pytest.skip(f"nvcc unavailable: {e}")
+    _, FP, FX = sky.compute_sky_delay_and_patterns(["L1", "H1", "V1"], "L1", 512.0, 20,
+                                                   healpix_order=3)
+    FP_t, FX_t = FP.T.astype(np.float32), FX.T.astype(np.float32)
+    valid = np.arange(0, FP_t.shape[0], 3, dtype=np.int64)
+    a = _lib.regulator_order(FP_t, FX_t, valid)
+    b = _lib.regulator_order(FP_t, FX_t, valid)
+    assert np.array_equal(a, b)
+    assert np.array_equal(np.sort(a), np.arange(valid.size))
+    with pytest.raises(ValueError):
+        _lib.regulator_order(FP_t, FX_t, np.array([0, FP_t.shape[0]], np.int64))

@@ -124,3 +124,39 @@ def test_batched_regulators_only(env, oracle_mod):
         ref = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
                                        reg["network_energy_threshold"], valid)
         assert np.float32(only[c]) == np.float32(ref), c
+
+
+@pytest.mark.parametrize("gamma", [0.02, 0.12, 0.2, 0.35])
+def test_regulator_early_decisions_are_exact(env, oracle_mod, gamma):
+    """The regulator stops a direction once its pass (running sum over the
+    threshold) or its fail (running sum plus a bound on the remaining
+    pixels under it) is certain; the count must still equal the reference's
+    for every cluster, at thresholds through the bulk of the directions."""
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch, SkyTables
+
+    reg = env["reg"]
+    FP_t, FX_t, ml = env["FP_t"], env["FX_t"], env["ml"]
+    tables = SkyTables.from_arrays(FP_t, FX_t, ml, None,
+                                   network_energy_threshold=reg["network_energy_threshold"],
+                                   gamma_regulator=gamma, delta_regulator=reg["delta_regulator"],
+                                   netCC=reg["netCC"])
+    rng = np.random.default_rng(int(gamma * 1000))
+    sizes = [1, 2, 17, 40, 333, 1500, 64, 900]
+    clusters = []
+    for k, P in enumerate(sizes):
+        rms = rng.uniform(0.3, 2.0, size=(P, 3)).astype(np.float32)
+        if k % 3 == 1 and P > 4:
+            rms[: P // 2, 2] = 1e-4                       # a nearly deaf detector
+        if k % 4 == 3:
+            rms[0] = 0.0                                  # a pixel with no weight at all
+        zero = np.zeros((41, 3, P), np.float32)
+        clusters.append((zero, zero, rms))
+    loop = BatchedSkyLoop(tables, ClusterBatch.from_clusters(clusters))
+    loop.upload()
+    got = loop.regulators()
+    n_sky = FP_t.shape[0]
+    valid = np.arange(n_sky, dtype=np.int64)
+    for c, (_, _, rms) in enumerate(clusters):
+        ref = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, gamma,
+                                       reg["network_energy_threshold"], valid)
+        assert np.float32(got[c]) == np.float32(ref), (gamma, c, got[c], ref)

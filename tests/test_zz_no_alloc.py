@@ -60,8 +60,8 @@ def test_noalloc_entry_point_matches_workspace_entry_point_twice():
     # the entry point with a caller workspace
     st_ref, res_ref, reg_ref = outputs()
     ws = torch.empty(L.pgw_workspace_bytes(3, 2 * K + 1, P, 1), dtype=torch.uint8, device=dev)
-    rc = L.pgw_sky_loop(*common, st_ref.data_ptr(), res_ref.data_ptr(), reg_ref.data_ptr(), None,
-                        ws.data_ptr(), ws.numel(), stream)
+    rc = L.pgw_sky_loop(*common, None, st_ref.data_ptr(), res_ref.data_ptr(), reg_ref.data_ptr(),
+                        None, ws.data_ptr(), ws.numel(), stream)
     assert rc == 0, L.pgw_last_error()
     torch.cuda.synchronize()
     ref = res_ref.cpu().numpy().view(np.dtype([("l", "<i8"), ("s", "<f4"), ("f", "<i4"),
