@@ -229,6 +229,8 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true",
                     help="skip the 4-detector HEALPix-8 lag pipeline field")
     ap.add_argument("--pipeline-clusters", type=int, default=1024)
+    ap.add_argument("--profile-regulator", action="store_true",
+                    help="with --profile: one regulator-only launch instead")
     ap.add_argument("--profile", action="store_true",
                     help="one eager launch of the batched loop and exit (for ncu)")
     args = ap.parse_args()
@@ -320,6 +322,13 @@ def main():
     loop.upload()
     loop.stream.synchronize()
 
+    if args.profile and args.profile_regulator:
+        with torch.cuda.stream(loop.stream):
+            reg_buf = torch.empty(args.clusters, dtype=torch.float64, device=dev)
+        loop.launch_regulators(reg_buf)
+        loop.stream.synchronize()
+        print(json.dumps({"profile": "one regulator-only launch", "clusters": args.clusters}))
+        return
     if args.profile:
         loop.launch()
         loop.stream.synchronize()
