@@ -229,6 +229,8 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true",
                     help="skip the 4-detector HEALPix-8 lag pipeline field")
     ap.add_argument("--pipeline-clusters", type=int, default=1024)
+    ap.add_argument("--profile-td", action="store_true",
+                    help="with --profile: one td-vector build of 1e6 pixels instead")
     ap.add_argument("--profile-regulator", action="store_true",
                     help="with --profile: one regulator-only launch instead")
     ap.add_argument("--profile", action="store_true",
@@ -295,6 +297,9 @@ def main():
     dev = torch.device("cuda", local)
     _lib.build()
     L = _lib.load()
+    if args.profile and args.profile_td:
+        print(json.dumps({"profile": "td build", **time_td_build(dev)}))
+        return
 
     ml, FP_t, FX_t = sky_tables_np(args.order)
     n_sky = ml.shape[1]
@@ -458,7 +463,7 @@ def main():
                                         "2 flops per FMA) in this run"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 4 * args.steps,  # init, pack, suffix sums, sky loop
             "clocks": clk,
             "plain": plain,
             "batched_vs_plain": (plain["ms"] / ms_per_step) if plain else None,
