@@ -28,24 +28,9 @@ namespace {
 
 constexpr double kSqrt2 = 1.4142135623730951;  // the double nearest sqrt(2)
 
-// float -> double, exact, on the integer pipe: a normal float's sign,
-// exponent (rebiased by 1023 - 127) and mantissa (shifted up 29 bits) are
-// the double's fields.  Zero, subnormal, infinite and NaN inputs take the
-// ordinary conversion.  The FIR kernels are bound by the float64 pipe, which
-// also executes the ordinary conversion; this keeps it for the products and
-// sums alone.
-__device__ __forceinline__ double widen(float x) {
-  const unsigned b = __float_as_uint(x);
-  const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return static_cast<double>(x);
-  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  const unsigned lo = (b & 7u) << 29;
-  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
-}
-
 __device__ __forceinline__ double plane_at(const float* __restrict__ plane, int64_t rows, int M1,
                                            int64_t r, int m) {
-  return (r < 0 || r >= rows) ? 0.0 : widen(__ldg(plane + r * M1 + m));
+  return (r < 0 || r >= rows) ? 0.0 : static_cast<double>(__ldg(plane + r * M1 + m));
 }
 
 __device__ __forceinline__ void fir(const float* __restrict__ plane, int64_t rows, int M1,
