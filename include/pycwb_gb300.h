@@ -157,7 +157,7 @@ int pgw_sky_loop(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP, const
  * cudaMalloc/cudaFree may synchronise the device, and a host framework that
  * owns the device memory (its own pool, a fixed budget) may forbid
  * allocations outside it.  Scratch comes from a static device array of
- * pgw_sky_loop_noalloc_max_scratch() bytes (8 MiB, enough for about 8,000
+ * pgw_sky_loop_noalloc_max_scratch() bytes (8 MiB, enough for about 7,800
  * pixels at n_ifo = 3 and n_delay = 41) that every GPU loading the library
  * holds until the process exits; a larger cluster is rejected with
  * PGW_ERR_WORKSPACE.  The call allocates nothing (no cudaMalloc/cudaFree, no
