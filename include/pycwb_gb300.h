@@ -289,6 +289,14 @@ int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* strea
  * the denominator of the td-amplitude build's roofline.  Synchronous. */
 int pgw_fp64_mul_add_peak(int iters, double* out_gops, double* out_ms, void* stream);
 
+/* Copy `bytes` from page-locked host memory (cudaHostAlloc'ed or registered)
+ * to device memory with a kernel instead of the copy engine, asynchronously
+ * on `stream`.  Input staging for the batched loop: the copy engine's first
+ * pass over a large host buffer right after a sky-loop launch was measured
+ * at 5-11 GB/s on GB300 (210 GB/s on later passes); SM loads keep many host
+ * pages in translation at once.  No counterpart in the reference. */
+int pgw_copy_from_host(void* dst, const void* host_src, size_t bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,8 @@ def load():
         L.pgw_calculate_dpf_batched.argtypes = [i32, i32, P, i64, i64, P, P, P, f64, f64, P, i64,
                                                 P, P, P, P, P, sz, P]
         L.pgw_calculate_dpf_batched.restype = ctypes.c_int
+        L.pgw_copy_from_host.argtypes = [P, P, sz, P]
+        L.pgw_copy_from_host.restype = ctypes.c_int
         L.pgw_fp64_mul_add_peak.argtypes = [i32, P, P, P]
         L.pgw_fp64_mul_add_peak.restype = ctypes.c_int
         L.pgw_sky_loop_noalloc.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64,

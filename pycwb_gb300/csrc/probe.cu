@@ -5,6 +5,8 @@
 // the host times the launch with CUDA events.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
 #include <string>
 
 #include "../../include/pycwb_gb300.h"
@@ -98,5 +100,59 @@ extern "C" int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, 
   const double fmas = static_cast<double>(n_sm) * 8 * 256 * iters * 16.0 * 8.0;
   *out_tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
   if (out_ms) *out_ms = ms;
+  return PGW_OK;
+}
+
+// Device-driven copy from page-locked host memory: every thread moves 16-byte
+// words (grid-stride), so the SMs keep many host-page translations in flight
+// at once.  Used by the batched loop's upload; the copy engine's path was
+// measured at 5-11 GB/s on its first pass over a buffer after a large sky-loop
+// launch (210 GB/s otherwise).
+namespace {
+__global__ void __launch_bounds__(256) copy_from_host_kernel(uint4* __restrict__ dst,
+                                                             const uint4* __restrict__ src,
+                                                             size_t n16) {
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n16; i += stride)
+    dst[i] = src[i];
+}
+__global__ void copy_tail_kernel(unsigned char* dst, const unsigned char* src, size_t n) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+}  // namespace
+
+extern "C" int pgw_copy_from_host(void* dst, const void* host_src, size_t bytes, void* stream) {
+  if (bytes == 0) return PGW_OK;
+  if (!dst || !host_src) return pgw::fail(PGW_ERR_BAD_ARGUMENT, "NULL pointer");
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host_src) != cudaSuccess || at.type != cudaMemoryTypeHost)
+    return pgw::fail(PGW_ERR_BAD_ARGUMENT, "source is not page-locked host memory");
+  const void* dev_src = at.devicePointer ? at.devicePointer : host_src;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0, n_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return pgw::fail(PGW_ERR_CUDA, "device query failed");
+  const bool aligned = (reinterpret_cast<uintptr_t>(dst) % 16 == 0) &&
+                       (reinterpret_cast<uintptr_t>(dev_src) % 16 == 0);
+  size_t head = 0;
+  if (aligned) {
+    const size_t n16 = bytes / 16;
+    head = n16 * 16;
+    if (n16) {
+      const unsigned blocks = static_cast<unsigned>(
+          std::min<size_t>((n16 + 255) / 256, static_cast<size_t>(n_sm) * 8));
+      copy_from_host_kernel<<<blocks, 256, 0, s>>>(static_cast<uint4*>(dst),
+                                                   static_cast<const uint4*>(dev_src), n16);
+    }
+  }
+  const size_t tail = bytes - head;
+  if (tail)
+    copy_tail_kernel<<<static_cast<unsigned>((tail + 255) / 256), 256, 0, s>>>(
+        static_cast<unsigned char*>(dst) + head, static_cast<const unsigned char*>(dev_src) + head,
+        tail);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return pgw::fail(PGW_ERR_CUDA, std::string("copy_from_host: ") + cudaGetErrorString(e));
   return PGW_OK;
 }

@@ -160,3 +160,21 @@ def test_regulator_early_decisions_are_exact(env, oracle_mod, gamma):
         ref = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, gamma,
                                        reg["network_energy_threshold"], valid)
         assert np.float32(got[c]) == np.float32(ref), (gamma, c, got[c], ref)
+
+
+@pytest.mark.parametrize("nbytes,offset", [(1 << 20, 0), ((1 << 22) + 13, 0), ((1 << 21) + 5, 3)])
+def test_copy_from_host_is_exact(env, nbytes, offset):
+    """pgw_copy_from_host (the upload path) moves bytes exactly, with
+    16-byte words where both ends are aligned and a byte tail otherwise."""
+    import torch
+    from pycwb_gb300 import _lib
+    src = torch.randint(0, 256, (nbytes + offset,), dtype=torch.uint8).pin_memory()
+    dst = torch.zeros(nbytes + offset, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    rc = _lib.load().pgw_copy_from_host(dst.data_ptr() + offset, src.data_ptr() + offset, nbytes,
+                                        s.cuda_stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got = dst.cpu()
+    assert torch.equal(got[offset:], src[offset:])
+    assert int(got[:offset].sum()) == 0
