@@ -26,7 +26,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the Makefile beside this file."""
-    srcs = [os.path.join(HERE, f) for f in ("skyscan_oracle.c", "tdamp_oracle.c", "Makefile")]
+    srcs = [os.path.join(HERE, f) for f in ("skyscan_oracle.c", "tdamp_oracle.c", "subnet_oracle.c",
+                                             "Makefile")]
     if force or not os.path.exists(LIB_PATH) or any(
             os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs):
         subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
@@ -48,8 +49,12 @@ def lib():
                                           P, i64, i32, P, P, P, P]
         L.oracle_batch_get_td_vecs.argtypes = [P, i64, P, P, i64, P, P, i32, i32, i32, i32, P,
                                                i32, P]
+        f32 = ctypes.c_float
+        for f in (L.oracle_subnet_sky_f32, L.oracle_subnet_sky_f64):
+            f.argtypes = [i32, i64, i64, P, P, P, P, P, i32, P, f32, f64, f64, P]
         for f in (L.oracle_calculate_dpf_f32, L.oracle_calculate_dpf_f64, L.oracle_scan_sky_f32,
-                  L.oracle_scan_sky_f64, L.oracle_batch_get_td_vecs):
+                  L.oracle_scan_sky_f64, L.oracle_batch_get_td_vecs, L.oracle_subnet_sky_f32,
+                  L.oracle_subnet_sky_f64):
             f.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -134,3 +139,18 @@ def batch_get_td_vecs(pixel_indices, padded00, padded90, T0, Tx, M, n_coeffs, K,
     if rc:
         raise ValueError("oracle batch_get_td_vecs failed")
     return out
+
+
+def optimze_sky_loc_from_td(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml,
+                            network_energy_threshold, e2or, subcut, precision="f32"):
+    """sub_net_cut.py:404-517; returns (l_max, stat, Em, Am, lm, Vm, suball, EE)."""
+    FP, FX, rms = _c(FP, np.float32), _c(FX, np.float32), _c(rms, np.float32)
+    td00, td90, ml = _c(td00, np.float32), _c(td90, np.float32), _c(ml, np.int32)
+    out = np.zeros(8, np.float64)
+    fn = lib().oracle_subnet_sky_f32 if precision == "f32" else lib().oracle_subnet_sky_f64
+    rc = fn(int(n_ifo), int(n_pix), int(n_sky), _p(FP), _p(FX), _p(rms), _p(td00), _p(td90),
+            int(td00.shape[0]), _p(ml), float(np.float32(network_energy_threshold)), float(e2or),
+            float(subcut), _p(out))
+    if rc:
+        raise ValueError(f"oracle_subnet_sky failed ({rc})")
+    return (int(out[0]), out[1], out[2], out[3], int(out[4]), int(out[5]), out[6], out[7])

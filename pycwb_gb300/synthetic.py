@@ -36,6 +36,23 @@ def regulators(n_ifo, acore=math.sqrt(2.0), gamma=0.5, delta=0.5, netCC=0.5, net
                 netEC_threshold=abs(netRHO) * abs(netRHO) * 2)
 
 
+def subnet_constants(n_ifo, acore=1.7, subcut=0.33):
+    """Constants of the sub-network cut (super_cluster.py:575-577,
+    sub_net_cut.py:190): network_energy_threshold = float32(2 Acore^2 nIFO)
+    and e2or from Acore as cWB's network::setAcore derives it
+    (pycwb/types/detector.py:1188-1217): p = Q(nIFO, Acore^2 nIFO) with Q the
+    regularised upper incomplete gamma, e2or = Q^-1(nIFO - 1, p)."""
+    from scipy.special import gammaincc, gammainccinv
+    n = int(max(1, n_ifo))
+    if n < 2:
+        e2or = float(max(0.0, acore))
+    else:
+        prob = float(np.clip(gammaincc(float(n), acore * acore * n), 1.0e-12, 1.0 - 1.0e-12))
+        e2or = float(gammainccinv(float(n - 1), prob))
+    return dict(network_energy_threshold=float(np.float32(2 * acore * acore * n)), e2or=e2or,
+                subcut=float(subcut))
+
+
 def make_rms(rng, n_pix, n_ifo):
     sigma = rng.uniform(0.5, 2.0, size=(n_ifo, n_pix))
     inv = 1.0 / sigma

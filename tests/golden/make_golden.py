@@ -15,9 +15,13 @@ NumPy scalars and carry a ``.dtype``.  The reference files are then loaded
 unmodified by file path and executed with NumPy scalar semantics.  The
 outputs are written as ``.npz`` fixtures next to this script.
 
+Also pycwb/modules/super_cluster_native/sub_net_cut.py (the sub-network-cut
+sky loop, optimze_sky_loc_from_td), whose other imports are given empty
+modules.
+
 Usage (needs the reference checkout; not used at test time)::
 
-    python tests/golden/make_golden.py /path/to/pycwb-reference
+    python tests/golden/make_golden.py /path/to/pycwb-reference [subnet]
 """
 
 from __future__ import annotations
@@ -108,6 +112,31 @@ def load_reference(ref_root):
     return dpf, stat, scan, tdk
 
 
+def load_subnet(ref_root, dpf):
+    """pycwb/modules/super_cluster_native/sub_net_cut.py under the stand-in.
+
+    Its module-level imports outside numpy/numba (the xtalk catalog reader,
+    pixel_data) serve other functions of the file; they get empty modules,
+    and `pycwb.modules.likelihoodWP.dpf` resolves to the reference's dpf.py
+    loaded above."""
+    for name in ("pycwb", "pycwb.modules", "pycwb.modules.likelihoodWP", "pycwb.modules.xtalk",
+                 "pycwb.modules.super_cluster_native"):
+        m = types.ModuleType(name)
+        m.__path__ = []
+        sys.modules[name] = m
+    sys.modules["pycwb.modules.likelihoodWP.dpf"] = dpf
+    for name, attrs in (("pycwb.modules.xtalk.monster", ("getXTalk_pixels_fast",)),
+                        ("pycwb.modules.xtalk.type", ("XTalk",)),
+                        ("pycwb.modules.likelihoodWP.pixel_data", ("load_data_from_pixels",))):
+        m = types.ModuleType(name)
+        for a in attrs:
+            setattr(m, a, object)
+        sys.modules[name] = m
+    path = os.path.join(ref_root, "pycwb", "modules", "super_cluster_native", "sub_net_cut.py")
+    return _load("pycwb.modules.super_cluster_native.sub_net_cut", path,
+                 "pycwb.modules.super_cluster_native")
+
+
 # --------------------------------------------------------------------------
 # cases
 # --------------------------------------------------------------------------
@@ -183,6 +212,41 @@ def _td_case(name, seed, M, n_coeffs, L, K, n_time, n_pix):
                 K=np.int64(K), J=np.int64(J))
 
 
+def _subnet_case(name, ifos, healpix_order, n_pix, K, seed, snr=20.0, acore=1.7, subcut=0.33,
+                 random_tables=False, n_sky=None):
+    from pycwb_gb300.synthetic import make_cluster, subnet_constants
+    from pycwb_gb300 import sky
+
+    rng = np.random.default_rng(seed)
+    n_ifo = len(ifos)
+    if random_tables:
+        n_sky = int(n_sky)
+        ml = rng.integers(-K, K + 1, size=(n_ifo, n_sky)).astype(np.int32)
+        ml[0] = 0
+        FP = rng.uniform(-1, 1, size=(n_ifo, n_sky))
+        FX = rng.uniform(-1, 1, size=(n_ifo, n_sky))
+    else:
+        ml, FP, FX = sky.compute_sky_delay_and_patterns(
+            ifos, ifos[0], 512.0, K, healpix_order=healpix_order)
+        n_sky = ml.shape[1]
+    FP_t = FP.T.astype(np.float32).copy()
+    FX_t = FX.T.astype(np.float32).copy()
+    td00, td90, rms, l_true = make_cluster(rng, ml, FP_t, FX_t, n_pix, K, snr)
+    c = subnet_constants(n_ifo, acore=acore, subcut=subcut)
+    return dict(name=name, n_ifo=n_ifo, n_pix=n_pix, n_sky=n_sky, FP=FP_t, FX=FX_t, rms=rms,
+                td00=td00, td90=td90, ml=ml, network_energy_threshold=np.float32(
+                    c["network_energy_threshold"]), e2or=np.float64(c["e2or"]),
+                subcut=np.float64(c["subcut"]), l_true=l_true)
+
+
+def run_subnet_case(snc, case):
+    out = snc.optimze_sky_loc_from_td(
+        case["n_ifo"], case["n_pix"], case["n_sky"], case["FP"], case["FX"], case["rms"],
+        case["td00"], case["td90"], case["ml"], case["network_energy_threshold"],
+        float(case["e2or"]), float(case["subcut"]))
+    return dict(out=np.array([float(x) for x in out], np.float64))
+
+
 def main(ref_root):
     ref = load_reference(ref_root)
     sky_cases = [
@@ -223,5 +287,31 @@ def main(ref_root):
         print(case["name"], out.shape, "->", os.path.relpath(path, REPO))
 
 
+def main_subnet(ref_root):
+    ref = load_reference(ref_root)
+    snc = load_subnet(ref_root, ref[0])
+    cases = [
+        _subnet_case("hlv_o2_p60", ["L1", "H1", "V1"], 2, 60, 20, seed=31),
+        _subnet_case("hlv_o3_p40_nocut", ["L1", "H1", "V1"], 3, 40, 20, seed=32, subcut=-1.0),
+        _subnet_case("hlvk_o2_p50", ["L1", "H1", "V1", "K1"], 2, 50, 20, seed=33, snr=30.0),
+        _subnet_case("hl_o2_p40", ["L1", "H1"], 2, 40, 20, seed=34),
+        _subnet_case("hlv_o2_p60_cut0", ["L1", "H1", "V1"], 2, 60, 20, seed=35, subcut=0.0,
+                     acore=1.2),
+        _subnet_case("rand_s120_p30", ["L1", "H1", "V1"], None, 30, 20, seed=36,
+                     random_tables=True, n_sky=120, subcut=-1.0, acore=1.0),
+        _subnet_case("hlv_o2_p3_quiet", ["L1", "H1", "V1"], 2, 3, 20, seed=37, snr=4.0),
+    ]
+    for case in cases:
+        res = run_subnet_case(snc, case)
+        path = os.path.join(HERE, f"subnet_{case['name']}.npz")
+        np.savez_compressed(path, **{k: v for k, v in case.items() if k != "name"}, **res)
+        print(case["name"], res["out"], "->", os.path.relpath(path, REPO))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYCWB_REFERENCE", ""))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYCWB_REFERENCE", "")
+    if len(sys.argv) > 2 and sys.argv[2] == "subnet":
+        main_subnet(root)
+    else:
+        main(root)
+        main_subnet(root)

@@ -81,3 +81,27 @@ def test_golden_edge_cases_are_present():
     assert int(z["l_max"]) == int(z["valid"][0]) and float(z["sky_stat_max"]) == 0.0
     z = np.load(os.path.join(GOLDEN, "sky_hlv_o2_p1.npz"))
     assert np.isnan(z["stats"][5]).any()                # 0/0 correlation where no pixel passes
+
+
+SUBNET_CASES = sorted(glob.glob(os.path.join(GOLDEN, "subnet_*.npz")))
+
+
+@pytest.mark.parametrize("path", SUBNET_CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_subnet_sky_loop_matches_reference_exactly(oracle_mod, path):
+    """optimze_sky_loc_from_td (sub_net_cut.py:404-517): the oracle returns
+    the reference's 8-tuple with identical float32 values."""
+    z = np.load(path)
+    got = oracle_mod.optimze_sky_loc_from_td(
+        int(z["n_ifo"]), int(z["n_pix"]), int(z["n_sky"]), z["FP"], z["FX"], z["rms"],
+        z["td00"], z["td90"], z["ml"], z["network_energy_threshold"], float(z["e2or"]),
+        float(z["subcut"]))
+    assert np.array_equal(np.array(got, np.float64), z["out"])
+
+
+def test_subnet_golden_cover_the_gates():
+    outs = {os.path.basename(p)[7:-4]: np.load(p) for p in SUBNET_CASES}
+    assert len(outs) >= 7
+    assert any(float(z["subcut"]) < 0 for z in outs.values())     # sky gate off
+    assert any(int(z["n_ifo"]) == 4 for z in outs.values())
+    assert any(int(z["n_ifo"]) == 2 for z in outs.values())
+    assert any(float(z["out"][1]) == 0.0 for z in outs.values())  # no direction qualified
