@@ -229,6 +229,37 @@ int pgw_batch_get_td_vecs(const int32_t* pixel_indices, int64_t n_pixels, const 
                           const double* phase, int M, int n_coeffs, int K, int J, float* out,
                           void* stream);
 
+/* Result of the sub-network-cut sky loop for one cluster: the reference's
+ * (l_max, stat, Em, Am, lm, Vm, suball, EE) with lm = l_max
+ * (pycwb/modules/super_cluster_native/sub_net_cut.py:517).  `key` is the
+ * loop's internal (statistic, direction) maximum; `status` carries
+ * device-detected errors as bits 1 << pgw_status. */
+typedef struct {
+  uint64_t key;
+  int64_t l_max;
+  float stat, Em, Am, suball, EE;
+  int32_t Vm;
+  int32_t status;
+  int32_t reserved;
+} pgw_subnet_result;
+
+/* Sub-network-cut sky loop for a batch of clusters in one launch:
+ * optimze_sky_loc_from_td (sub_net_cut.py:404-517) on every cluster, over
+ * all n_sky directions (the reference's MIN_SKYRES_HEALPIX grid).  Cluster
+ * layout as in pgw_sky_loop_batched (pix_offsets/td_offsets may be NULL for
+ * one cluster of total_pix pixels); FP, FX (n_sky, n_ifo); ml (n_ifo, n_sky);
+ * network_energy_threshold = float32(2 Acore^2 n_ifo) (:190), e2or and subcut
+ * as the reference takes them (subcut < 0 turns the sky gate off).  out:
+ * n_clusters results.  Every float32 operation is rounded as the reference's
+ * (NumPy scalar semantics, no contraction), so the results equal the
+ * reference's bit for bit on its own arithmetic. */
+int pgw_subnet_sky_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
+                           const int64_t* td_offsets, int64_t total_pix, int64_t n_sky,
+                           const float* FP, const float* FX, const float* rms_all,
+                           const float* td00_all, const float* td90_all, int n_delay,
+                           const int32_t* ml, float network_energy_threshold, double e2or,
+                           double subcut, pgw_subnet_result* out, void* stream);
+
 /* td-amplitude vectors written straight into the batched scan's inputs: the
  * amplitudes of pgw_batch_get_td_vecs for the n_pixels pixels of one
  * (WDM plane, detector `ifo`) go to cluster dst_cluster[p], local pixel
