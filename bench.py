@@ -226,6 +226,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shape")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-td", action="store_true")
+    ap.add_argument("--no-subnet", action="store_true",
+                    help="skip the sub-network-cut sky loop field")
     ap.add_argument("--no-fast", action="store_true",
                     help="skip timing the approximate-division variant")
     ap.add_argument("--no-pipeline", action="store_true",
@@ -453,6 +455,7 @@ def main():
     torch.cuda.empty_cache()
     pipeline = (time_pipeline(dev, args.seed + 1000 * rank, args.pipeline_clusters)
                 if not args.no_pipeline else None)
+    subnet = time_subnet(dev, args.seed + 7 + 1000 * rank) if not args.no_subnet else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -497,6 +500,7 @@ def main():
             "adjoint": adjoint,
             "td_build": td_build,
             "pipeline": pipeline,
+            "subnet": subnet,
             "selected": {"found": int(found.sum()),
                          "l_max_equals_injected": int(np.sum(l_max == l_true))},
             "step_ms": step_ms,
@@ -682,6 +686,81 @@ def time_pipeline(dev, seed, n_clusters=1024, steps=2):
         "note": "wall clock per lag through LagPipeline.run (td amplitudes never leave "
                 "the device; rms in, per-cluster results out)",
     }
+
+
+def time_subnet(dev, seed, n_clusters=1024, n_loud=200, order=4, reps=3):
+    """Sub-network-cut sky loop (sub_net_cut.py:404-517) for a lag's
+    superclusters: n_clusters clusters of their n_loud loudest pixels
+    (LOUD = 200, utils.py:705-711) over the HEALPix-4 grid (MIN_SKYRES_HEALPIX
+    = 4), L1/H1/V1, K = 20, Acore 1.7, subcut 0.33; one launch of
+    pgw_subnet_sky_batched, device-resident inputs, CUDA-event timed; the
+    float32 oracle (one core) on 4 of the clusters for the CPU figure."""
+    import torch
+
+    from pycwb_gb300 import _device as dv
+    from pycwb_gb300 import _lib, sky
+    from pycwb_gb300.likelihoodWP.batched import ClusterBatch
+    from pycwb_gb300.synthetic import make_batch_device, subnet_constants
+
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(IFOS, "L1", 512.0, K_TD, healpix_order=order)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    n_sky = ml.shape[1]
+    c = subnet_constants(len(IFOS), acore=1.7, subcut=0.33)
+    sizes = np.full(n_clusters, n_loud, np.int64)
+    b = ClusterBatch(len(IFOS), 2 * K_TD + 1, sizes)
+    td00, td90, rms, _, _ = make_batch_device(seed, sizes, ml, FP_t, FX_t, K_TD, device=dev)
+    b.td00.copy_(td00)
+    b.td90.copy_(td90)
+    b.rms.copy_(rms)
+    s = dv.stream()
+    L = _lib.load()
+    FPd, FXd = torch.from_numpy(FP_t).to(dev), torch.from_numpy(FX_t).to(dev)
+    mld = torch.from_numpy(ml.astype(np.int32)).to(dev)
+    pix_off = torch.from_numpy(b.pix_offsets).to(dev)
+    td_off = torch.from_numpy(b.td_offsets).to(dev)
+    out = torch.empty((n_clusters, 48), dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()   # the generator wrote the device inputs
+
+    def launch():
+        rc = L.pgw_subnet_sky_batched(len(IFOS), n_clusters, pix_off.data_ptr(), td_off.data_ptr(),
+                                      b.total_pix, n_sky, FPd.data_ptr(), FXd.data_ptr(),
+                                      rms.data_ptr(), td00.data_ptr(), td90.data_ptr(),
+                                      2 * K_TD + 1, mld.data_ptr(),
+                                      float(np.float32(c["network_energy_threshold"])),
+                                      c["e2or"], c["subcut"], out.data_ptr(), s.cuda_stream)
+        if rc:
+            raise RuntimeError(L.pgw_last_error().decode())
+    launch()
+    s.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        launch()
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    evals = n_clusters * n_sky
+    from oracle import oracle as orc   # the CPU baseline (test infrastructure)
+    t0 = time.perf_counter()
+    n_cpu = 4
+    for k in range(n_cpu):
+        a_, b_ = int(b.td_offsets[k]), int(b.td_offsets[k + 1])
+        shp = (2 * K_TD + 1, len(IFOS), n_loud)
+        p0, p1 = int(b.pix_offsets[k]), int(b.pix_offsets[k + 1])
+        orc.optimze_sky_loc_from_td(len(IFOS), n_loud, n_sky, FP_t, FX_t, b.rms[p0:p1].numpy(),
+                                    b.td00[a_:b_].numpy().reshape(shp),
+                                    b.td90[a_:b_].numpy().reshape(shp), ml,
+                                    c["network_energy_threshold"], c["e2or"], c["subcut"])
+    cpu_s = time.perf_counter() - t0
+    res = out.cpu().numpy().view(np.dtype([("key", "<u8"), ("l_max", "<i8"), ("f", "<f4", 5),
+                                           ("Vm", "<i4"), ("status", "<i4"), ("r", "<i4")]))
+    return {"workload": f"{n_clusters} clusters x {n_loud} loudest pixels, HEALPix {order} "
+                        f"({n_sky} directions), L1/H1/V1, K={K_TD}, Acore 1.7, subcut 0.33",
+            "ms": ms, "cluster_sky_evals_per_s": evals / (ms * 1e-3),
+            "cpu_oracle_evals_per_s": n_cpu * n_sky / cpu_s, "cpu_cores": 1,
+            "cpu_sample": f"{n_cpu} clusters, float32 oracle, one thread",
+            "selected": int((res["key"].reshape(-1) != 0).sum())}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):
