@@ -233,6 +233,8 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true",
                     help="skip the 4-detector HEALPix-8 lag pipeline field")
     ap.add_argument("--pipeline-clusters", type=int, default=1024)
+    ap.add_argument("--profile-subnet", action="store_true",
+                    help="with --profile: the sub-network-cut sky loop field only")
     ap.add_argument("--profile-td", action="store_true",
                     help="with --profile: one td-vector build of 1e6 pixels instead")
     ap.add_argument("--profile-regulator", action="store_true",
@@ -303,6 +305,9 @@ def main():
     L = _lib.load()
     if args.profile and args.profile_td:
         print(json.dumps({"profile": "td build", **time_td_build(dev)}))
+        return
+    if args.profile and args.profile_subnet:
+        print(json.dumps({"profile": "sub-network sky loop", **time_subnet(dev, args.seed, reps=1)}))
         return
 
     ml, FP_t, FX_t = sky_tables_np(args.order)
