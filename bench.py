@@ -451,6 +451,7 @@ def main():
     if not args.no_plain:
         plain = time_plain(L, loop, tables, batch, shape, dev)
         plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
+        plain["roofline_frac"] = (useful_ops / (plain["ms"] * 1e-3) / 1e12 / peak) if peak else None
 
     adjoint = time_adjoint(loop, res, batch, args.order, dev) if not args.no_adjoint else None
     td_build = time_td_build(dev) if not args.no_td else None
