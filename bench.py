@@ -787,7 +787,7 @@ def time_plain(L, loop, tables, batch, shape, dev):
         a, b = int(batch.td_offsets[c]), int(batch.pix_offsets[c])
         ptrs.append((int(batch.sizes[c]), loop.td00.data_ptr() + 4 * a, loop.td90.data_ptr() + 4 * a,
                      loop.rms.data_ptr() + 4 * batch.n_ifo * b))
-    shp = ctypes.byref(shape) if shape is not None else None
+    shp = None   # the default one-cluster shape, as sky_loop / scan_sky_for_best_fit use it
 
     def one(c):
         P, t0, t9, rm = ptrs[c]
@@ -813,7 +813,8 @@ def time_plain(L, loop, tables, batch, shape, dev):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     return {"ms": ms, "launches": batch.n_clusters * 3,
-            "note": "same kernel, one pgw_sky_loop per cluster, device-resident, 1 timed pass"}
+            "note": "same kernel, one pgw_sky_loop per cluster with the default one-cluster "
+                    "launch shape, device-resident, 1 timed pass"}
 
 
 if __name__ == "__main__":
