@@ -812,7 +812,7 @@ def time_plain(L, loop, tables, batch, shape, dev):
     e1.record(s)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    return {"ms": ms, "launches": batch.n_clusters * 3,
+    return {"ms": ms, "launches": batch.n_clusters * 4,  # init, pack, suffix sums, sky loop
             "note": "same kernel, one pgw_sky_loop per cluster with the default one-cluster "
                     "launch shape, device-resident, 1 timed pass"}
 
