@@ -250,9 +250,10 @@ typedef struct {
  * one cluster of total_pix pixels); FP, FX (n_sky, n_ifo); ml (n_ifo, n_sky);
  * network_energy_threshold = float32(2 Acore^2 n_ifo) (:190), e2or and subcut
  * as the reference takes them (subcut < 0 turns the sky gate off).  out:
- * n_clusters results.  Every float32 operation is rounded as the reference's
- * (NumPy scalar semantics, no contraction), so the results equal the
- * reference's bit for bit on its own arithmetic. */
+ * n_clusters results (1 <= n_clusters <= 65535 per call).  Every float32
+ * operation is rounded as the reference's (NumPy scalar semantics, no
+ * contraction), so the results equal the reference's bit for bit on its own
+ * arithmetic. */
 int pgw_subnet_sky_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                            const int64_t* td_offsets, int64_t total_pix, int64_t n_sky,
                            const float* FP, const float* FX, const float* rms_all,
