@@ -261,6 +261,19 @@ int pgw_subnet_sky_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets
                            const int32_t* ml, float network_energy_threshold, double e2or,
                            double subcut, pgw_subnet_result* out, void* stream);
 
+/* Per-segment sky tables on the device for a HEALPix RING grid of order
+ * healpix_order (12 * 4^order directions): FP, FX (n_sky, n_ifo) float32
+ * antenna patterns at psi = 0 and ml (n_ifo, n_sky) int32 delay indices
+ * clip(rint((n . b_i) / c_light * sample_rate), -td_size, td_size), from each
+ * detector's 3x3 response tensor (response, host, n_ifo x 9 float64,
+ * row-major) and baseline to the reference detector (baseline, host,
+ * n_ifo x 3 float64, metres).  Replaces compute_sky_delay_and_patterns
+ * (pycwb/types/detector.py:1243-1329) for HEALPix grids; outputs are device
+ * pointers, written asynchronously on `stream`. */
+int pgw_sky_tables_healpix(int healpix_order, int n_ifo, const double* response,
+                           const double* baseline, double c_light, double sample_rate,
+                           int td_size, float* FP, float* FX, int32_t* ml, void* stream);
+
 /* td-amplitude vectors written straight into the batched scan's inputs: the
  * amplitudes of pgw_batch_get_td_vecs for the n_pixels pixels of one
  * (WDM plane, detector `ifo`) go to cluster dst_cluster[p], local pixel

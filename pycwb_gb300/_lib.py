@@ -19,7 +19,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
-SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu"]
+SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu"]
 HEADERS = ["common.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -118,6 +118,8 @@ def load():
         L.pgw_subnet_sky_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, f32,
                                              f64, f64, P, P]
         L.pgw_subnet_sky_batched.restype = ctypes.c_int
+        L.pgw_sky_tables_healpix.argtypes = [i32, i32, P, P, f64, f64, i32, P, P, P, P]
+        L.pgw_sky_tables_healpix.restype = ctypes.c_int
         L.pgw_copy_from_host.argtypes = [P, P, sz, P]
         L.pgw_copy_from_host.restype = ctypes.c_int
         L.pgw_fp64_mul_add_peak.argtypes = [i32, P, P, P]

@@ -212,3 +212,37 @@ def compute_sky_delay_and_patterns(ifos, ref_ifo, sample_rate, td_size,
                         -td_size, td_size)
         FP[i], FX[i] = d.antenna_pattern_geo(phi_geo, lat, 0.0)
     return ml, FP, FX
+
+
+def compute_sky_delay_and_patterns_device(ifos, ref_ifo, sample_rate, td_size, healpix_order,
+                                          device="cuda"):
+    """compute_sky_delay_and_patterns for a HEALPix grid, built on the GPU
+    (pgw_sky_tables_healpix): (ml (n_ifo, n_sky) int32, FP_t, FX_t
+    (n_sky, n_ifo) float32) as CUDA tensors, in the layouts the sky scan
+    takes."""
+    import torch
+
+    from . import _device as dv
+    from . import _lib
+
+    dets = [DetectorSite(d) if isinstance(d, str) else d for d in ifos]
+    if not dets:
+        raise ValueError("No detectors provided")
+    ref = next((i for i, d in enumerate(dets) if d.name == ref_ifo), 0)
+    resp = np.ascontiguousarray(np.stack([d.response for d in dets]).reshape(len(dets), 9),
+                                np.float64)
+    base = np.ascontiguousarray(np.stack([d.vertex - dets[ref].vertex for d in dets]), np.float64)
+    n_sky = healpix_npix(healpix_order)
+    dev = torch.device(device)
+    s = dv.begin()
+    with torch.cuda.stream(s):
+        FP = torch.empty((n_sky, len(dets)), dtype=torch.float32, device=dev)
+        FX = torch.empty((n_sky, len(dets)), dtype=torch.float32, device=dev)
+        ml = torch.empty((len(dets), n_sky), dtype=torch.int32, device=dev)
+    rc = _lib.load().pgw_sky_tables_healpix(int(healpix_order), len(dets), resp.ctypes.data,
+                                            base.ctypes.data, float(C_LIGHT), float(sample_rate),
+                                            int(max(1, td_size)), FP.data_ptr(), FX.data_ptr(),
+                                            ml.data_ptr(), s.cuda_stream)
+    _lib.check(rc, "sky_tables_healpix")
+    dv.end(s, FP, FX, ml)
+    return ml, FP, FX
