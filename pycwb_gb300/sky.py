@@ -225,6 +225,8 @@ def compute_sky_delay_and_patterns_device(ifos, ref_ifo, sample_rate, td_size, h
     from . import _device as dv
     from . import _lib
 
+    if int(healpix_order) < 1:
+        raise ValueError("healpix_order must be >= 1 (order 0 selects the host's non-HEALPix grid)")
     dets = [DetectorSite(d) if isinstance(d, str) else d for d in ifos]
     if not dets:
         raise ValueError("No detectors provided")

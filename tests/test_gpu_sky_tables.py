@@ -25,7 +25,7 @@ def sky():
 
 
 @pytest.mark.parametrize("ifos,order,rate,K", [
-    (("L1", "H1", "V1"), 0, 512.0, 20),
+    (("L1", "H1", "V1"), 1, 512.0, 20),
     (("L1", "H1", "V1"), 3, 512.0, 20),
     (("L1", "H1", "V1", "K1"), 5, 2048.0, 67),
     (("L1", "H1", "V1"), 7, 512.0, 20),
