@@ -123,3 +123,34 @@ def test_refinement_and_timing(lag):
     again = lag["pipe"].run(refine=False)       # a second run rebuilds the same inputs
     assert np.array_equal(again.scan.l_max, out.scan.l_max)
     assert np.array_equal(again.scan.sky_stat_max, out.scan.sky_stat_max)
+
+
+def test_per_detector_pixel_rows(lag, oracle_mod):
+    """cluster_pixels given as (n_ifo, P) rows (each detector's own, e.g.
+    time-shifted, pixels): every detector's td block comes from its row."""
+    from pycwb_gb300.likelihoodWP.lag_pipeline import LagPipeline
+    rng = np.random.default_rng(9)
+    D = 2 * K + 1
+    pixels2 = []
+    for c, p in enumerate(lag["pixels"]):
+        M = int(lag["level"][c])
+        n_cells = lag["planes"][M][0].padded00.shape[0] * (M + 1)
+        rows = np.stack([np.roll(p, i) if i % 2 == 0 else
+                         rng.choice(n_cells, size=p.size, replace=False).astype(np.int32)
+                         for i in range(len(IFOS))])
+        pixels2.append(rows)
+    pipe = LagPipeline(lag["tables"], lag["planes"], lag["level"], pixels2, lag["rms"], K)
+    pipe.build_td()
+    pipe.loop.stream.synchronize()
+    td00 = pipe.loop.td00.cpu().numpy()
+    b = pipe.batch
+    for c in range(b.n_clusters):
+        P = pixels2[c].shape[1]
+        a = int(b.td_offsets[c])
+        blk = td00[a:a + D * len(IFOS) * P].reshape(D, len(IFOS), P)
+        for i, t in enumerate(lag["planes"][int(lag["level"][c])]):
+            v = oracle_mod.batch_get_td_vecs(pixels2[c][i], t.padded00.cpu().numpy(),
+                                             t.padded90.cpu().numpy(), t.T0.cpu().numpy(),
+                                             t.Tx.cpu().numpy(), t.M, t.n_coeffs, K, t.J)
+            assert np.array_equal(blk[:, i, :].view(np.uint32),
+                                  np.ascontiguousarray(v[:, :D].T).view(np.uint32)), (c, i)
