@@ -134,7 +134,8 @@ def test_per_detector_pixel_rows(lag, oracle_mod):
     pixels2 = []
     for c, p in enumerate(lag["pixels"]):
         M = int(lag["level"][c])
-        n_cells = lag["planes"][M][0].padded00.shape[0] * (M + 1)
+        t0 = lag["planes"][M][0]
+        n_cells = (t0.padded00.shape[0] - 2 * t0.n_coeffs) * (M + 1)   # unpadded time slices
         rows = np.stack([np.roll(p, i) if i % 2 == 0 else
                          rng.choice(n_cells, size=p.size, replace=False).astype(np.int32)
                          for i in range(len(IFOS))])
@@ -143,14 +144,18 @@ def test_per_detector_pixel_rows(lag, oracle_mod):
     pipe.build_td()
     pipe.loop.stream.synchronize()
     td00 = pipe.loop.td00.cpu().numpy()
+    td90 = pipe.loop.td90.cpu().numpy()
     b = pipe.batch
     for c in range(b.n_clusters):
         P = pixels2[c].shape[1]
         a = int(b.td_offsets[c])
         blk = td00[a:a + D * len(IFOS) * P].reshape(D, len(IFOS), P)
+        blk90 = td90[a:a + D * len(IFOS) * P].reshape(D, len(IFOS), P)
         for i, t in enumerate(lag["planes"][int(lag["level"][c])]):
             v = oracle_mod.batch_get_td_vecs(pixels2[c][i], t.padded00.cpu().numpy(),
                                              t.padded90.cpu().numpy(), t.T0.cpu().numpy(),
                                              t.Tx.cpu().numpy(), t.M, t.n_coeffs, K, t.J)
             assert np.array_equal(blk[:, i, :].view(np.uint32),
                                   np.ascontiguousarray(v[:, :D].T).view(np.uint32)), (c, i)
+            assert np.array_equal(blk90[:, i, :].view(np.uint32),
+                                  np.ascontiguousarray(v[:, D:].T).view(np.uint32)), (c, i)
