@@ -237,6 +237,10 @@ def main():
                     help="with --profile: the sub-network-cut sky loop field only")
     ap.add_argument("--profile-td", action="store_true",
                     help="with --profile: one td-vector build of 1e6 pixels instead")
+    ap.add_argument("--no-wdm", action="store_true",
+                    help="skip the WDM transform (strain -> padded planes) field")
+    ap.add_argument("--profile-wdm", action="store_true",
+                    help="with --profile: the WDM transform field only")
     ap.add_argument("--profile-regulator", action="store_true",
                     help="with --profile: one regulator-only launch instead")
     ap.add_argument("--profile", action="store_true",
@@ -305,6 +309,9 @@ def main():
     L = _lib.load()
     if args.profile and args.profile_td:
         print(json.dumps({"profile": "td build", **time_td_build(dev)}))
+        return
+    if args.profile and args.profile_wdm:
+        print(json.dumps({"profile": "wdm transform", **time_wdm(dev, reps=1)}))
         return
     if args.profile and args.profile_subnet:
         print(json.dumps({"profile": "sub-network sky loop", **time_subnet(dev, args.seed, reps=1)}))
@@ -455,6 +462,7 @@ def main():
 
     adjoint = time_adjoint(loop, res, batch, args.order, dev) if not args.no_adjoint else None
     td_build = time_td_build(dev) if not args.no_td else None
+    wdm_field = time_wdm(dev) if not args.no_wdm else None
     found, l_max = res.found.copy(), res.l_max.copy()
     res.maps = None                  # release the 4096-cluster buffers first
     del loop, res
@@ -505,6 +513,7 @@ def main():
             "fast_math_variant": fast,
             "adjoint": adjoint,
             "td_build": td_build,
+            "wdm": wdm_field,
             "pipeline": pipeline,
             "subnet": subnet,
             "selected": {"found": int(found.sum()),
@@ -627,6 +636,82 @@ def time_td_build(dev, n_pix=1_000_000, M=64, nc=20, K=20):
             "pixels_per_s": n_pix / (ms * 1e-3),
             "roofline": td_roofline(_lib.load(), n_pix * (2 * K + 1), 2 * nc + 1, ms),
             "note": "float64 accumulation, bit-identical to the reference"}
+
+
+WDM_LAYERS = (16, 32, 64, 128, 256, 512)
+
+
+def wdm_instructions(M: int, n_filter: int, n_time: int) -> int:
+    """float64 instructions of one transform (an FMA counted once): per time
+    slice the fold's 2M * 2k + 1 FMAs (the 2 * 2kM + 1 filter taps, k = (n_filter
+    - 1) / 2M) and 8 per butterfly of the radix-2 FFT of length 2M (M log2(2M)
+    butterflies: a complex multiply as 2 multiplies + 2 FMAs, then 4 adds)."""
+    M2 = 2 * M
+    kf = (n_filter - 1) // M2
+    return n_time * (M2 * 2 * kf + 1 + 8 * M * int(round(math.log2(M2))))
+
+
+def time_wdm(dev, n_ifo=4, duration=600.0, rate=512.0, nc=12, L=4, beta=4, prec=10, reps=3):
+    """T2: every detector's strain to the padded float32 WDM planes of every
+    level (16-512 layers), as the reference's per-segment td-inputs cache
+    (td_vector_batch.py:35-144); CUDA-event timed on the launching stream.
+    Basis and TD filters are designed on the host once per level (timed
+    apart); the oracle's numpy transform of one detector is the CPU line."""
+    import torch
+    from pycwb_gb300 import _lib, wdm
+    from oracle import wdm_oracle
+
+    t0 = time.perf_counter()
+    bases = [wdm.WDM(M, M, beta, prec) for M in WDM_LAYERS]
+    for b in bases:
+        b.set_td_filter(nc, L)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    n = int(duration * rate)
+    rng = np.random.default_rng(3)
+    strains = [torch.from_numpy(rng.standard_normal(n)).to(dev) for _ in range(n_ifo)]
+    s = torch.cuda.current_stream(dev)
+
+    def run():
+        return [[b.td_inputs(x, stream=s) for x in strains] for b in bases]
+
+    run()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        out = run()
+        e1.record(s)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    instr = n_ifo * sum(wdm_instructions(b.M, b.m_H, wdm.t2w_n_time(n, b.M)) for b in bases)
+    nbytes = n_ifo * sum(8 * n + 2 * 4 * (wdm.t2w_n_time(n, b.M) + 2 * nc) * (b.M + 1)
+                         for b in bases)
+    peak = fp64_peak(_lib.load())
+    achieved = instr / (t * 1e-3) / 1e9
+    c0 = time.perf_counter()
+    for b in bases:
+        wdm_oracle.t2w(strains[0].cpu().numpy(), b.M, b.filter)
+    cpu_ms = (time.perf_counter() - c0) * 1e3 * n_ifo
+    del out
+    return {"workload": f"{n_ifo} detectors x {duration:.0f} s at {rate:.0f} Hz, "
+                        f"{WDM_LAYERS[0]}-{WDM_LAYERS[-1]} layers ({len(WDM_LAYERS)} levels), "
+                        f"beta {beta}, precision {prec}, TD filters {2 * nc + 1} taps, upTDF {L}",
+            "transforms": n_ifo * len(bases), "ms": t, "launches": n_ifo * len(bases),
+            "samples_per_s": n_ifo * len(bases) * n / (t * 1e-3),
+            "host_design_ms": host_ms, "bytes": nbytes,
+            "achieved_gbs": nbytes / (t * 1e-3) / 1e9,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "G ops/s",
+                         "frac": achieved / peak if peak else None, "instructions": instr,
+                         "peak_source": "measured: pgw_fp64_mul_add_peak in this run; "
+                                        "float64 instructions, an FMA counted once"},
+            "cpu_oracle_ms": cpu_ms, "cpu_cores": 1,
+            "cpu_note": "oracle numpy transform (fold + numpy.fft.rfft) of one detector's "
+                        "levels, times the detector count",
+            "note": "writes the zero-padded float32 planes the td build reads "
+                    "(t2w + prepare_td_inputs in one kernel)"}
 
 
 PIPE_IFOS = ["L1", "H1", "V1", "K1"]

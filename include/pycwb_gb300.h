@@ -334,6 +334,24 @@ int pgw_fp32_fma_peak(int iters, double* out_tflops, double* out_ms, void* strea
  * the denominator of the td-amplitude build's roofline.  Synchronous. */
 int pgw_fp64_mul_add_peak(int iters, double* out_gops, double* out_ms, void* stream);
 
+/* WDM forward transform of one series, both quadratures: cWB's
+ * WDM::t2w(MM = -1) (cwb-core/WDM.cc:1384-1535), which the reference calls
+ * through wdm_wavelet's WDM.t2w (pycwb/utils/td_vector_batch.py:80) and then
+ * pads (pycwb/types/time_frequency_map.py:482-521).  ts: n_ts float64
+ * samples (device); M: layers, a power of two in [1, 4096]; filter: the
+ * basis filter's n_filter float64 coefficients (device; n_filter - 1 a
+ * multiple of 2M, n_ts > n_filter).  Outputs (device, either pair may be
+ * NULL): map00/map90 (n_time, M+1) float64 with n_time = pgw_wdm_n_time(n_ts,
+ * M), row n = time slice n; padded00/padded90 (n_time + 2 n_pad, M+1)
+ * float32, the same values between n_pad zero rows on each side (the
+ * TDBatchInputs planes of pgw_batch_get_td_vecs).  Asynchronous on `stream`. */
+int pgw_wdm_t2w(const double* ts, int64_t n_ts, int M, const double* filter, int64_t n_filter,
+                double* map00, double* map90, float* padded00, float* padded90, int n_pad,
+                void* stream);
+
+/* Time slices of pgw_wdm_t2w: ceil(n_samples / M) (-1 for M < 1). */
+int64_t pgw_wdm_n_time(int64_t n_samples, int M);
+
 /* Copy `bytes` from page-locked host memory (cudaHostAlloc'ed or registered)
  * to device memory with a kernel instead of the copy engine, asynchronously
  * on `stream`.  Input staging for the batched loop: the copy engine's first

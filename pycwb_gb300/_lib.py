@@ -19,7 +19,8 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
-SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu"]
+SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu",
+           "wdm.cu"]
 HEADERS = ["common.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -120,6 +121,10 @@ def load():
         L.pgw_subnet_sky_batched.restype = ctypes.c_int
         L.pgw_sky_tables_healpix.argtypes = [i32, i32, P, P, f64, f64, i32, P, P, P, P]
         L.pgw_sky_tables_healpix.restype = ctypes.c_int
+        L.pgw_wdm_t2w.argtypes = [P, i64, i32, P, i64, P, P, P, P, i32, P]
+        L.pgw_wdm_t2w.restype = ctypes.c_int
+        L.pgw_wdm_n_time.argtypes = [i64, i32]
+        L.pgw_wdm_n_time.restype = i64
         L.pgw_copy_from_host.argtypes = [P, P, sz, P]
         L.pgw_copy_from_host.restype = ctypes.c_int
         L.pgw_fp64_mul_add_peak.argtypes = [i32, P, P, P]
