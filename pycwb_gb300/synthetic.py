@@ -244,3 +244,122 @@ def make_lag(seed, ifos, ml, FP_t, FX_t, *, layers=(16, 32, 64, 128, 256, 512), 
             t.padded90.index_put_((rows_t, cols_t), torch.from_numpy(
                 s90[:, i].astype(np.float32)).to(device), accumulate=True)
     return planes, level, pixels, rms, l_true
+
+
+def make_strain_lag(seed, ifos, ml, FP_t, FX_t, td_rate, *, layers=(16, 32, 64, 128, 256, 512),
+                    duration=600.0, rate=512.0, n_inj=200, n_clusters=1024, size_lo=50,
+                    size_hi=5000, snr_lo=8.0, snr_hi=40.0, f_lo=32.0, f_hi=224.0, q=9.0,
+                    beta_order=4, precision=10, td_size=12, device="cuda"):
+    """A synthetic lag built from strain: LagPipeline inputs through the WDM.
+
+    Every detector gets `duration` s of white unit-variance noise at `rate`
+    Hz plus n_inj injections from grid directions l_true: sine-Gaussians
+    (f0 ~ U[f_lo, f_hi], quality q, random phase and ellipticity) and, one in
+    five, Gaussian pulses (width 4-16 ms), scaled to a network SNR ~
+    U[snr_lo, snr_hi].  Detector i sees h(t + ml[i, l_true] / td_rate)
+    projected on F+/Fx of the direction, the arrival-time convention of the
+    td amplitudes (the amplitude at delay d is that of the series delayed
+    by d).  The series are transformed on the device (pycwb_gb300.wdm: every
+    level of `layers`, TD filters of 2 td_size + 1 taps at upTDF = td_rate /
+    rate), as the reference's td inputs cache does (td_vector_batch.py:35-144).
+    The first n_inj clusters are the injections' (pixels: the P loudest of a
+    time-frequency box around the injection at a random level, P ~
+    log-uniform[size_lo, size_hi]), the others noise boxes picked the same
+    way.  rms is 1/sqrt(n_ifo) for every pixel (equal white noise).
+    Returns (planes, cluster_level, cluster_pixels, rms, l_true, info);
+    l_true is -1 for noise clusters, info carries the injections and the
+    transform's device time (t2w_ms)."""
+    import torch
+
+    from .wdm import WDM, t2w_n_time
+
+    up = int(round(td_rate / rate))
+    if up < 1 or abs(up * rate - td_rate) > 1e-9 * td_rate:
+        raise ValueError("td_rate must be an integer multiple of rate")
+    rng = np.random.default_rng(seed)
+    n_ifo = len(ifos)
+    n_sky = ml.shape[1]
+    n = int(round(duration * rate))
+    x = rng.standard_normal((n_ifo, n))
+    t = np.arange(n) / rate
+    margin = 4.0
+    kinds = np.where(rng.random(n_inj) < 0.8, 0, 1)
+    t0s = rng.uniform(margin, duration - margin, n_inj)
+    f0s = rng.uniform(f_lo, f_hi, n_inj)
+    snrs = rng.uniform(snr_lo, snr_hi, n_inj)
+    l_inj = rng.integers(n_sky, size=n_inj)
+    for k in range(n_inj):
+        if kinds[k] == 0:
+            tau = q / (math.sqrt(2.0) * math.pi * f0s[k])
+        else:
+            tau = rng.uniform(0.004, 0.016)
+        ph, ell = rng.uniform(0, 2 * math.pi), rng.uniform(0.0, 1.0)
+        a = max(0, int((t0s[k] - 0.2 - 6 * tau) * rate))
+        b = min(n, int((t0s[k] + 0.2 + 6 * tau) * rate) + 1)
+        fp = FP_t[l_inj[k]].astype(np.float64)
+        fx = FX_t[l_inj[k]].astype(np.float64)
+        h = np.zeros((n_ifo, b - a))
+        for i in range(n_ifo):
+            u = t[a:b] + ml[i, l_inj[k]] / td_rate - t0s[k]
+            env = np.exp(-(u / tau) ** 2)
+            if kinds[k] == 0:
+                hp = env * np.sin(2 * math.pi * f0s[k] * u + ph)
+                hx = ell * env * np.cos(2 * math.pi * f0s[k] * u + ph)
+            else:
+                hp, hx = env, np.zeros_like(env)
+            h[i] = fp[i] * hp + fx[i] * hx
+        e = float(np.sum(h * h))
+        if e > 0.0:
+            x[:, a:b] += h * (snrs[k] / math.sqrt(e))
+
+    dev = torch.device(device)
+    strains = [torch.from_numpy(x[i]).to(dev) for i in range(n_ifo)]
+    s = torch.cuda.current_stream(dev)
+    bases = {}
+    for M in layers:
+        w = WDM(int(M), int(M), beta_order, precision)
+        w.set_td_filter(td_size, up)
+        bases[int(M)] = w
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    planes = {M: [w.td_inputs(xs, stream=s) for xs in strains] for M, w in bases.items()}
+    e1.record(s)
+    e1.synchronize()
+    t2w_ms = e0.elapsed_time(e1)
+
+    nc = int(td_size)
+    energy = {}
+    for M, per in planes.items():
+        N = t2w_n_time(n, M)
+        energy[M] = sum((p.padded00[nc:nc + N].double() ** 2 + p.padded90[nc:nc + N].double() ** 2)
+                        for p in per)
+
+    sizes = log_uniform_sizes(rng, n_clusters, size_lo, size_hi)
+    level = rng.choice(np.asarray(layers, np.int64), size=n_clusters)
+    pixels, rms, l_true = [], [], np.full(n_clusters, -1, np.int64)
+    for c in range(n_clusters):
+        M = int(level[c])
+        E = energy[M]
+        N, n_f = E.shape
+        P = int(min(sizes[c], N * n_f // 2))
+        wf = int(min(n_f, max(1, math.ceil(math.sqrt(2 * P)))))
+        wt = int(min(N, math.ceil(2 * P / wf)))
+        P = min(P, wt * wf)
+        if c < n_inj:
+            l_true[c] = l_inj[c]
+            nc0 = int(round(t0s[c] * rate / M))
+            mc0 = int(round(f0s[c] / (rate / (2.0 * M)))) if kinds[c] == 0 else 0
+            n0 = int(np.clip(nc0 - wt // 2, 0, N - wt))
+            m0 = int(np.clip(mc0 - wf // 2, 0, n_f - wf))
+        else:
+            n0 = int(rng.integers(0, N - wt + 1))
+            m0 = int(rng.integers(0, n_f - wf + 1))
+        box = E[n0:n0 + wt, m0:m0 + wf].reshape(-1)
+        top = torch.topk(box, P).indices.cpu().numpy()
+        nn, mm = n0 + top // wf, m0 + top % wf
+        pixels.append((nn * n_f + mm).astype(np.int32))
+        rms.append(np.full((P, n_ifo), 1.0 / math.sqrt(n_ifo), np.float32))
+    info = {"t0": t0s, "f0": f0s, "snr": snrs, "kind": kinds, "t2w_ms": t2w_ms,
+            "samples": n, "bases": bases}
+    return planes, level, pixels, rms, l_true, info
