@@ -237,6 +237,8 @@ def main():
                     help="with --profile: the sub-network-cut sky loop field only")
     ap.add_argument("--profile-td", action="store_true",
                     help="with --profile: one td-vector build of 1e6 pixels instead")
+    ap.add_argument("--profile-pipeline", action="store_true",
+                    help="with --profile: the lag pipeline field only")
     ap.add_argument("--no-wdm", action="store_true",
                     help="skip the WDM transform (strain -> padded planes) field")
     ap.add_argument("--profile-wdm", action="store_true",
@@ -309,6 +311,10 @@ def main():
     L = _lib.load()
     if args.profile and args.profile_td:
         print(json.dumps({"profile": "td build", **time_td_build(dev)}))
+        return
+    if args.profile and args.profile_pipeline:
+        print(json.dumps({"profile": "lag pipeline",
+                          **time_pipeline(dev, args.seed, args.pipeline_clusters)}))
         return
     if args.profile and args.profile_wdm:
         print(json.dumps({"profile": "wdm transform", **time_wdm(dev, reps=1)}))
@@ -775,6 +781,8 @@ def time_pipeline(dev, seed, n_clusters=1024, steps=2):
         "t2w_ms_per_segment": info["t2w_ms"],
         "injections_located_within_2deg": int(np.sum(ang <= 2.0)),
         "injection_median_angle_deg": float(np.median(ang)),
+        "injection_median_angle_deg_snr_above_20": float(np.median(
+            ang[info["snr"][inj] > 20.0])) if np.any(info["snr"][inj] > 20.0) else None,
         "clusters": n_clusters, "total_pix": pipe.total_pix, "n_sky": n_sky,
         "steps": steps, "ms_per_lag": wall * 1e3, **st,
         "cluster_sky_evals_per_s": n_clusters * n_sky / (wall),

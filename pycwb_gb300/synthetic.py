@@ -263,9 +263,10 @@ def make_strain_lag(seed, ifos, ml, FP_t, FX_t, td_rate, *, layers=(16, 32, 64, 
     level of `layers`, TD filters of 2 td_size + 1 taps at upTDF = td_rate /
     rate), as the reference's td inputs cache does (td_vector_batch.py:35-144).
     The first n_inj clusters are the injections' (pixels: the P loudest of a
-    time-frequency box around the injection at a random level, P ~
-    log-uniform[size_lo, size_hi]), the others noise boxes picked the same
-    way.  rms is 1/sqrt(n_ifo) for every pixel (equal white noise).
+    time-frequency box around the injection, at the level whose time step
+    best matches the injection's duration, P ~ log-uniform[size_lo,
+    10 size_lo]), the others noise boxes at random levels with P ~
+    log-uniform[size_lo, size_hi], picked the same way.  rms is 1/sqrt(n_ifo) for every pixel (equal white noise).
     Returns (planes, cluster_level, cluster_pixels, rms, l_true, info);
     l_true is -1 for noise clusters, info carries the injections and the
     transform's device time (t2w_ms)."""
@@ -288,11 +289,10 @@ def make_strain_lag(seed, ifos, ml, FP_t, FX_t, td_rate, *, layers=(16, 32, 64, 
     f0s = rng.uniform(f_lo, f_hi, n_inj)
     snrs = rng.uniform(snr_lo, snr_hi, n_inj)
     l_inj = rng.integers(n_sky, size=n_inj)
+    taus = np.where(kinds == 0, q / (math.sqrt(2.0) * math.pi * f0s),
+                    rng.uniform(0.004, 0.016, n_inj))
     for k in range(n_inj):
-        if kinds[k] == 0:
-            tau = q / (math.sqrt(2.0) * math.pi * f0s[k])
-        else:
-            tau = rng.uniform(0.004, 0.016)
+        tau = float(taus[k])
         ph, ell = rng.uniform(0, 2 * math.pi), rng.uniform(0.0, 1.0)
         a = max(0, int((t0s[k] - 0.2 - 6 * tau) * rate))
         b = min(n, int((t0s[k] + 0.2 + 6 * tau) * rate) + 1)
@@ -337,6 +337,12 @@ def make_strain_lag(seed, ifos, ml, FP_t, FX_t, td_rate, *, layers=(16, 32, 64, 
 
     sizes = log_uniform_sizes(rng, n_clusters, size_lo, size_hi)
     level = rng.choice(np.asarray(layers, np.int64), size=n_clusters)
+    lay = np.asarray(layers, np.float64)
+    for k in range(min(n_inj, n_clusters)):
+        # the resolution whose time step best matches the injection's duration
+        level[k] = int(lay[np.argmin(np.abs(np.log(lay / rate / (2.0 * taus[k]))))])
+    sizes[:n_inj] = log_uniform_sizes(rng, min(n_inj, n_clusters), size_lo,
+                                      max(size_lo, min(size_hi, 10 * size_lo)))
     pixels, rms, l_true = [], [], np.full(n_clusters, -1, np.int64)
     for c in range(n_clusters):
         M = int(level[c])
@@ -360,6 +366,6 @@ def make_strain_lag(seed, ifos, ml, FP_t, FX_t, td_rate, *, layers=(16, 32, 64, 
         nn, mm = n0 + top // wf, m0 + top % wf
         pixels.append((nn * n_f + mm).astype(np.int32))
         rms.append(np.full((P, n_ifo), 1.0 / math.sqrt(n_ifo), np.float32))
-    info = {"t0": t0s, "f0": f0s, "snr": snrs, "kind": kinds, "t2w_ms": t2w_ms,
+    info = {"t0": t0s, "f0": f0s, "snr": snrs, "kind": kinds, "tau": taus, "t2w_ms": t2w_ms,
             "samples": n, "bases": bases}
     return planes, level, pixels, rms, l_true, info
