@@ -125,6 +125,97 @@ int oracle_calculate_dpf_f32(const float* FP, const float* FX, const float* rms,
   return ORC_OK;
 }
 
+/* One pixel of one direction through load_data_from_td, avx_GW_ps,
+ * avx_ort_ps and avx_stat_ps (sky_stat.py:74-89, 157-189, 264-288, 357-405):
+ * every per-pixel quantity the scan accumulates and the statistics at l_max
+ * read back. */
+typedef struct {
+  float et, msk, ee, EE, osi, oco, ec, gn, rn, ll;
+  int32_t mk;
+  float s[ORC_MAXIFO], S[ORC_MAXIFO];
+} pix32_t;
+
+static inline void pixel32(int I, const float* v0, const float* v9, const dpf32_t* dp,
+                           float rr, float RR, float ethr32, pix32_t* o) {
+  const dpf32_t d = *dp;
+  /* load_data_from_td, sky_stat.py:74-89 */
+  float aa = 0.f, AA = 0.f;
+  for (int i = 0; i < I; ++i) { aa += v0[i] * v0[i]; AA += v9[i] * v9[i]; }
+  float e = aa + AA + 1e-12f;
+  int32_t mk = e > ethr32 ? 1 : 0;
+  float et = mk ? e : 0.0f;
+
+  /* avx_GW_ps, sky_stat.py:157-189 */
+  float xp = 0.f, XP = 0.f, xx = 0.f, XX = 0.f;
+  for (int i = 0; i < I; ++i) {
+    xp += v0[i] * d.f[i]; XP += v9[i] * d.f[i];
+    xx += v0[i] * d.F[i]; XX += v9[i] * d.F[i];
+  }
+  float t = d.ni * (xp * xp + XP * XP);
+  t = t / (et + 1e-9f);
+  float g = sqrtf(t) * rr - d.fp;                        /* :164 */
+  g = g > 0.0f ? g : 0.0f;                               /* :165 */
+  double fd = (double)mk / (double)((d.fp + g) + 1e-9f); /* :166, int32/float32 -> float64 */
+  double h = (double)xp * fd, Hh = (double)XP * fd;      /* :168-169 */
+  h = h * h + Hh * Hh;                                   /* :170 */
+  float H2 = xx * xx + XX * XX;                          /* :171 */
+  double Fd = sqrt((double)H2 / (h + (double)1e-9f));    /* :172 */
+  float R = 0.1f + RR / (et + 1e-9f);                    /* :173 */
+  float G = (float)Fd * R - d.fx;                        /* :174 */
+  G = G > 0.0f ? G : 0.0f;                               /* :175 */
+  double Gd = (double)mk / (double)((d.fx + G) + 1e-9f); /* :176 */
+  float au = (float)((double)xp * fd), AU = (float)((double)XP * fd);   /* :178-179 */
+  float av = (float)((double)xx * Gd), AV = (float)((double)XX * Gd);   /* :180-181 */
+  double a_ = fd * (double)d.fp + Gd * (double)d.fx;     /* :183 */
+  float msk = (float)((a_ + (double)mk) - (double)1.0f); /* :185 */
+  for (int i = 0; i < I; ++i) {                          /* :187-189 */
+    o->s[i] = d.f[i] * au + d.F[i] * av;
+    o->S[i] = d.f[i] * AU + d.F[i] * AV;
+  }
+  const float* s = o->s;
+  const float* S = o->S;
+
+  /* avx_ort_ps, sky_stat.py:264-288 */
+  float a2 = 0.f, A2 = 0.f, aA = 0.f;
+  for (int i = 0; i < I; ++i) { a2 += s[i] * s[i]; A2 += S[i] * S[i]; aA += s[i] * S[i]; }
+  float osi = aA * 2.0f;
+  float oco = a2 - A2;
+  float oet = a2 + A2 + 1e-21f;
+  float occ = oco * oco, oss = osi * osi;
+  float onn = sqrtf(occ + oss);
+  o->ee = (oet + onn) / 2.0f;
+  o->EE = (oet - onn) / 2.0f;
+  occ = oco / (onn + 1e-21f);
+  float sgn = osi > 0.0f ? 1.0f : -1.0f;
+  osi = sqrtf((1.0f - occ) / 2.0f);
+  oco = sqrtf((1.0f + occ) / 2.0f) * sgn;
+
+  /* avx_stat_ps, sky_stat.py:357-405 */
+  float c = 0.f, C = 0.f, ss = 0.f, SS = 0.f, r0 = 0.f, R0 = 0.f, xs = 0.f, XS = 0.f;
+  for (int i = 0; i < I; ++i) {
+    float s_ = s[i] * oco + S[i] * osi;
+    float x_ = v0[i] * oco + v9[i] * osi;
+    float S_ = S[i] * oco - s[i] * osi;
+    float X_ = v9[i] * oco - v0[i] * osi;
+    float a = s_ * x_, A = S_ * X_;
+    xs += a; XS += A;
+    c += a * a; C += A * A;
+    ss += s_ * s_; SS += S_ * S_;
+    float q0 = s[i] - v0[i], q9 = S[i] - v9[i];
+    r0 += q0 * q0; R0 += q9 * q9;
+  }
+  int mks = msk >= 0.0f ? 1 : 0;                         /* :385 */
+  c = c / (xs * xs + 1e-9f);
+  C = C / (XS * XS + 1e-9f);
+  o->ll = (float)mks * (ss + SS);
+  ss = ss * (1.0f - c);
+  SS = SS * (1.0f - C);
+  o->ec = (float)mks * (ss + SS);
+  o->gn = (float)(mks * 2.0) * msk;
+  o->rn = (float)mks * (r0 + R0);
+  o->et = et; o->mk = mk; o->msk = msk; o->osi = osi; o->oco = oco;
+}
+
 /* One sky direction of scan_sky_for_best_fit (sky_scan.py:98-179) fused into
  * a single pass over the pixels; every accumulator keeps pixel order. */
 static inline int scan_sky32(int I, int64_t P, int64_t l, const float* FP, const float* FX,
@@ -153,92 +244,21 @@ static inline int scan_sky32(int I, int64_t P, int64_t l, const float* FP, const
       v0[i] = td00[((int64_t)row[i] * I + i) * P + j];
       v9[i] = td90[((int64_t)row[i] * I + i) * P + j];
     }
-    /* load_data_from_td, sky_stat.py:74-89 */
-    float aa = 0.f, AA = 0.f;
-    for (int i = 0; i < I; ++i) { aa += v0[i] * v0[i]; AA += v9[i] * v9[i]; }
-    float e = aa + AA + 1e-12f;
-    int32_t mk = e > ethr32 ? 1 : 0;
-    float et = mk ? e : 0.0f;
-    EE += et;
-
-    /* dpf_np_loops_vec, dpf.py:396-446 */
-    dpf32_t d;
+    dpf32_t d;                                           /* dpf_np_loops_vec, dpf.py:396-446 */
     dpf_pixel32(Fp, Fx, rms + j * I, I, &d);
-
-    /* avx_GW_ps, sky_stat.py:157-189 */
-    float xp = 0.f, XP = 0.f, xx = 0.f, XX = 0.f;
-    for (int i = 0; i < I; ++i) {
-      xp += v0[i] * d.f[i]; XP += v9[i] * d.f[i];
-      xx += v0[i] * d.F[i]; XX += v9[i] * d.F[i];
-    }
-    float t = d.ni * (xp * xp + XP * XP);
-    t = t / (et + 1e-9f);
-    float g = sqrtf(t) * rr - d.fp;                      /* :164 */
-    g = g > 0.0f ? g : 0.0f;                             /* :165 */
-    double fd = (double)mk / (double)((d.fp + g) + 1e-9f);   /* :166, int32/float32 -> float64 */
-    double h = (double)xp * fd, Hh = (double)XP * fd;    /* :168-169 */
-    h = h * h + Hh * Hh;                                 /* :170 */
-    float H2 = xx * xx + XX * XX;                        /* :171 */
-    double Fd = sqrt((double)H2 / (h + (double)1e-9f));  /* :172 */
-    float R = 0.1f + RR / (et + 1e-9f);                  /* :173 */
-    float G = (float)Fd * R - d.fx;                      /* :174 */
-    G = G > 0.0f ? G : 0.0f;                             /* :175 */
-    double Gd = (double)mk / (double)((d.fx + G) + 1e-9f);   /* :176 */
-    float au = (float)((double)xp * fd), AU = (float)((double)XP * fd);   /* :178-179 */
-    float av = (float)((double)xx * Gd), AV = (float)((double)XX * Gd);   /* :180-181 */
-    double a_ = fd * (double)d.fp + Gd * (double)d.fx;   /* :183 */
-    Mo += mk;                                            /* :184 */
-    float msk = (float)((a_ + (double)mk) - (double)1.0f);   /* :185 */
-    float s[ORC_MAXIFO], S[ORC_MAXIFO];
-    for (int i = 0; i < I; ++i) {                        /* :187-189 */
-      s[i] = d.f[i] * au + d.F[i] * av;
-      S[i] = d.f[i] * AU + d.F[i] * AV;
-    }
-
-    /* avx_ort_ps, sky_stat.py:264-288 */
-    float a2 = 0.f, A2 = 0.f, aA = 0.f;
-    for (int i = 0; i < I; ++i) { a2 += s[i] * s[i]; A2 += S[i] * S[i]; aA += s[i] * S[i]; }
-    float osi = aA * 2.0f;
-    float oco = a2 - A2;
-    float occ = oco * oco, oss = osi * osi;
-    float onn = sqrtf(occ + oss);
-    occ = oco / (onn + 1e-21f);
-    float sgn = osi > 0.0f ? 1.0f : -1.0f;
-    osi = sqrtf((1.0f - occ) / 2.0f);
-    oco = sqrtf((1.0f + occ) / 2.0f) * sgn;
-
-    /* avx_stat_ps, sky_stat.py:357-405 */
-    float c = 0.f, C = 0.f, ss = 0.f, SS = 0.f, r0 = 0.f, R0 = 0.f, xs = 0.f, XS = 0.f;
-    for (int i = 0; i < I; ++i) {
-      float s_ = s[i] * oco + S[i] * osi;
-      float x_ = v0[i] * oco + v9[i] * osi;
-      float S_ = S[i] * oco - s[i] * osi;
-      float X_ = v9[i] * oco - v0[i] * osi;
-      float a = s_ * x_, A = S_ * X_;
-      xs += a; XS += A;
-      c += a * a; C += A * A;
-      ss += s_ * s_; SS += S_ * S_;
-      float q0 = s[i] - v0[i], q9 = S[i] - v9[i];
-      r0 += q0 * q0; R0 += q9 * q9;
-    }
-    int mks = msk >= 0.0f ? 1 : 0;                       /* :385 */
-    c = c / (xs * xs + 1e-9f);
-    C = C / (XS * XS + 1e-9f);
-    float ll = (float)mks * (ss + SS);
-    ss = ss * (1.0f - c);
-    SS = SS * (1.0f - C);
-    float ec = (float)mks * (ss + SS);
-    float gn = (float)(mks * 2.0) * msk;
-    float rn = (float)mks * (r0 + R0);
-    float a2e = 2.0f * fabsf(ec);
-    float An = rn + gn + 1e-9f;
-    float ccn = ec / (a2e + An);
-    Lr += ll * ccn;
-    LL += ll; EC += ec; GN += gn; RN += rn;
-    NNc += ec > 1e-9f ? 1.0f : 0.0f;
+    pix32_t q;
+    pixel32(I, v0, v9, &d, rr, RR, ethr32, &q);
+    EE += q.et;
+    Mo += q.mk;                                          /* sky_stat.py:184 */
+    float a2e = 2.0f * fabsf(q.ec);
+    float An = q.rn + q.gn + 1e-9f;
+    float ccn = q.ec / (a2e + An);
+    Lr += q.ll * ccn;
+    LL += q.ll; EC += q.ec; GN += q.gn; RN += q.rn;
+    NNc += q.ec > 1e-9f ? 1.0f : 0.0f;
 
     /* sky_scan.py:148-153 */
-    if (msk > 0.0f) { ee += et; ffw += d.fp * et; FFw += d.fx * et; }
+    if (q.msk > 0.0f) { ee += q.et; ffw += d.fp * q.et; FFw += d.fx * q.et; }
   }
   const float Eo = EE / 2.0f;                            /* sky_stat.py:89 */
   const float Cr = 2.0f * Lr / (LL + 1e-9f);             /* sky_stat.py:407 */
@@ -520,4 +540,55 @@ int oracle_scan_sky_f64(int n_ifo, int64_t n_pix, int64_t n_sky, const float* FP
   }
   free(best);
   return err;
+}
+
+/* Every per-pixel quantity of one direction l (float32 reference arithmetic),
+ * for the statistics at the sky maximum (sky_statistics.py:94-133): the
+ * delayed data v0/v9 (I x P), the DPF vectors f/F (P x I) and norms fp/fx/ni,
+ * the thresholded energy et and mask mk (load_data_from_td), the float mask
+ * msk and signal s/S (I x P, avx_GW_ps), the packet energies ee/EE and
+ * rotation osi/oco (avx_ort_ps), and ec/gn/rn (avx_stat_ps). */
+int oracle_direction_pixels_f32(int n_ifo, int64_t n_pix, int64_t l, const float* FP,
+                                const float* FX, const float* rms, const float* td00,
+                                const float* td90, int n_delay, int64_t n_sky, const int32_t* ml,
+                                const float* REG, double network_energy_threshold,
+                                float* v0o, float* v9o, float* fo, float* Fo, float* fpo, float* fxo,
+                                float* nio, float* eto, int32_t* mko, float* msko, float* so,
+                                float* So, float* eeo, float* EEo, float* osio, float* ocoo,
+                                float* eco, float* gno, float* rno) {
+  const int I = n_ifo;
+  const int64_t P = n_pix;
+  if (I < 1 || I > ORC_MAXIFO || P < 0 || n_sky < 1 || l < 0 || l >= n_sky) return ORC_BAD_SHAPE;
+  const int off = n_delay / 2;
+  int row[ORC_MAXIFO];
+  for (int i = 0; i < I; ++i) {
+    int d = ml[(int64_t)i * n_sky + l] + off;
+    if (d < 0 || d >= n_delay) return ORC_BAD_DELAY;
+    row[i] = d;
+  }
+  const float ethr32 = (float)network_energy_threshold;
+  for (int64_t j = 0; j < P; ++j) {
+    float v0[ORC_MAXIFO], v9[ORC_MAXIFO];
+    for (int i = 0; i < I; ++i) {
+      v0[i] = td00[((int64_t)row[i] * I + i) * P + j];
+      v9[i] = td90[((int64_t)row[i] * I + i) * P + j];
+      v0o[i * P + j] = v0[i];
+      v9o[i * P + j] = v9[i];
+    }
+    dpf32_t d;
+    dpf_pixel32(FP + l * I, FX + l * I, rms + j * I, I, &d);
+    pix32_t q;
+    pixel32(I, v0, v9, &d, REG[0], REG[1], ethr32, &q);
+    for (int i = 0; i < I; ++i) {
+      fo[j * I + i] = d.f[i];
+      Fo[j * I + i] = d.F[i];
+      so[i * P + j] = q.s[i];
+      So[i * P + j] = q.S[i];
+    }
+    fpo[j] = d.fp; fxo[j] = d.fx; nio[j] = d.ni;
+    eto[j] = q.et; mko[j] = q.mk; msko[j] = q.msk;
+    eeo[j] = q.ee; EEo[j] = q.EE; osio[j] = q.osi; ocoo[j] = q.oco;
+    eco[j] = q.ec; gno[j] = q.gn; rno[j] = q.rn;
+  }
+  return ORC_OK;
 }

@@ -19,9 +19,13 @@ Also pycwb/modules/super_cluster_native/sub_net_cut.py (the sub-network-cut
 sky loop, optimze_sky_loc_from_td), whose other imports are given empty
 modules.
 
+Also pycwb/modules/likelihoodWP/sky_statistics.py (statistics at the sky
+maximum, compute_statistics_at_sky_position) with its packet operations,
+on synthetic xtalk overlaps (the overlap catalog is not in the checkout).
+
 Usage (needs the reference checkout; not used at test time)::
 
-    python tests/golden/make_golden.py /path/to/pycwb-reference [subnet]
+    python tests/golden/make_golden.py /path/to/pycwb-reference [subnet|skystat]
 """
 
 from __future__ import annotations
@@ -31,6 +35,7 @@ import math
 import os
 import sys
 import types
+import zlib
 
 import numpy as np
 
@@ -308,10 +313,92 @@ def main_subnet(ref_root):
         print(case["name"], res["out"], "->", os.path.relpath(path, REPO))
 
 
+def load_skystat(ref_root):
+    """pycwb/modules/likelihoodWP/sky_statistics.py (statistics at l_max) with
+    packet_ops.py and typing.py under the stand-in; the xtalk type it imports
+    for annotations only gets an empty module."""
+    lwp = os.path.join(ref_root, "pycwb", "modules", "likelihoodWP")
+    for name in ("pycwb", "pycwb.modules", "pycwb.modules.xtalk"):
+        if name not in sys.modules:
+            m = types.ModuleType(name)
+            m.__path__ = []
+            sys.modules[name] = m
+    m = types.ModuleType("pycwb.modules.xtalk.type")
+    m.XTalk = object
+    sys.modules["pycwb.modules.xtalk.type"] = m
+    _load("ref_lwp.typing", os.path.join(lwp, "typing.py"), "ref_lwp")
+    _load("ref_lwp.packet_ops", os.path.join(lwp, "packet_ops.py"), "ref_lwp")
+    return _load("ref_lwp.sky_statistics", os.path.join(lwp, "sky_statistics.py"), "ref_lwp")
+
+
+def synthetic_xtalk(rng, n_pix, n_nbr=4, scale=0.05):
+    """Packed xtalk rows for a cluster (the catalog itself is not in the
+    reference checkout): each pixel overlaps itself with (1, 0, 0, 1) and up
+    to n_nbr other pixels with small random coefficients."""
+    rows, lookup = [], np.zeros((n_pix, 2), np.int64)
+    for i in range(n_pix):
+        start = len(rows)
+        rows.append([i, 0, 0, 0, 1.0, 0.0, 0.0, 1.0])
+        if n_pix > 1:
+            for j in rng.choice(n_pix, size=min(n_nbr, n_pix), replace=False):
+                if j != i:
+                    rows.append([j, 0, 0, 0, *rng.normal(0.0, scale, 4)])
+        lookup[i] = (start, len(rows))
+    return np.asarray(rows, np.float32), lookup
+
+
+SKYSTAT_SCALARS = ("Gn", "Ec", "Dc", "Rc", "Eh", "Es", "Np", "Em", "Lm", "norm", "cc", "rho",
+                   "xrho", "Lo", "Eo")
+SKYSTAT_ARRAYS = ("energy_array_plus", "energy_array_cross", "pixel_mask",
+                  "gaussian_noise_correction", "coherent_energy", "noise_amplitude_00",
+                  "noise_amplitude_90", "pd", "pD", "ps", "pS", "S_snr", "f", "F")
+
+
+def main_skystat(ref_root):
+    ref = load_reference(ref_root)
+    ss = load_skystat(ref_root)
+    cases = [
+        ("hlv_o2_p40", _sky_case("hlv_o2_p40", ["L1", "H1", "V1"], 2, 40, 20, seed=41), {}),
+        ("hlvk_o2_p30", _sky_case("hlvk_o2_p30", ["L1", "H1", "V1", "K1"], 2, 30, 20, seed=42,
+                                  snr=25.0), {}),
+        ("hl_o2_p32", _sky_case("hl_o2_p32", ["L1", "H1"], 2, 32, 20, seed=43), {}),
+        ("hlv_o2_p60_xgb", _sky_case("hlv_o2_p60_xgb", ["L1", "H1", "V1"], 2, 60, 20, seed=44,
+                                     snr=30.0), {"xgb_rho_mode": True}),
+        ("hlv_o2_p40_offmax", _sky_case("hlv_o2_p40_offmax", ["L1", "H1", "V1"], 2, 40, 20,
+                                        seed=45), {"direction": 17}),
+        ("hlv_o2_p5_quiet", _sky_case("hlv_o2_p5_quiet", ["L1", "H1", "V1"], 2, 5, 20, seed=46,
+                                      snr=6.0), {}),
+    ]
+    for name, case, opt in cases:
+        res = run_sky_case(ref, case)
+        rng = np.random.default_rng(zlib.crc32(name.encode()))
+        xt, look = synthetic_xtalk(rng, case["n_pix"])
+        l = int(opt.get("direction", res["l_max"]))
+        out = ss.compute_statistics_at_sky_position(
+            l, case["n_ifo"], case["n_pix"], case["FP"], case["FX"], case["rms"], case["td00"],
+            case["td90"], case["ml"], res["REG"], case["network_energy_threshold"], xt, look,
+            xgb_rho_mode=bool(opt.get("xgb_rho_mode", False)))
+        arrays = {f"out_{k}": np.asarray(getattr(out, k)) for k in SKYSTAT_ARRAYS}
+        arrays.update({f"out_{k}_r": np.asarray(getattr(out, k)[0]) for k in ("p00_POL", "p90_POL")})
+        arrays.update({f"out_{k}_a": np.asarray(getattr(out, k)[1]) for k in ("p00_POL", "p90_POL")})
+        dst = os.path.join(HERE, f"skystat_{name}.npz")
+        np.savez_compressed(
+            dst, n_ifo=case["n_ifo"], n_pix=case["n_pix"], FP=case["FP"], FX=case["FX"],
+            rms=case["rms"], td00=case["td00"], td90=case["td90"], ml=case["ml"], REG=res["REG"],
+            network_energy_threshold=case["network_energy_threshold"], sky_idx=l, xtalk=xt,
+            xtalk_lookup=look, xgb_rho_mode=bool(opt.get("xgb_rho_mode", False)),
+            scalars=np.array([float(getattr(out, k)) for k in SKYSTAT_SCALARS]),
+            N_pix_effective=float(out.N_pix_effective), **arrays)
+        print(dst, {k: float(getattr(out, k)) for k in ("Ec", "Lm", "rho", "Em")})
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYCWB_REFERENCE", "")
     if len(sys.argv) > 2 and sys.argv[2] == "subnet":
         main_subnet(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "skystat":
+        main_skystat(root)
     else:
         main(root)
         main_subnet(root)
+        main_skystat(root)

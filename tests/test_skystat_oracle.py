@@ -1,0 +1,57 @@
+"""The statistics-at-l_max oracle (oracle/skystat_oracle.py) against golden
+vectors written by the reference's own compute_statistics_at_sky_position
+(pycwb/modules/likelihoodWP/sky_statistics.py:26-262; tests/golden/
+skystat_*.npz from tests/golden/make_golden.py, on synthetic xtalk
+overlaps).  The per-pixel part comes from the C oracle, bit-exact to the
+reference's sky scan; the packet part follows NumPy's rounding rules.  Every
+float32 statistic equals the reference's bit for bit; the float64 packet
+amplitudes may differ in the last bit where a BLAS dot product of the xtalk
+overlaps sums in another order (tolerance 1e-14 of the array's scale).
+"""
+
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "skystat_*.npz")))
+SCALARS = ("Gn", "Ec", "Dc", "Rc", "Eh", "Es", "Np", "Em", "Lm", "norm", "cc", "rho", "xrho",
+           "Lo", "Eo")
+ARRAYS = ("energy_array_plus", "energy_array_cross", "pixel_mask", "gaussian_noise_correction",
+          "coherent_energy", "noise_amplitude_00", "noise_amplitude_90", "pd", "pD", "ps", "pS",
+          "S_snr", "f", "F")
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_statistics_at_sky_position_match_reference(oracle_mod, path):
+    from oracle import skystat_oracle
+    z = np.load(path)
+    out = skystat_oracle.statistics_at_sky_position(
+        int(z["sky_idx"]), int(z["n_ifo"]), int(z["n_pix"]), z["FP"], z["FX"], z["rms"],
+        z["td00"], z["td90"], z["ml"], z["REG"], float(z["network_energy_threshold"]),
+        z["xtalk"], z["xtalk_lookup"], xgb_rho_mode=bool(z["xgb_rho_mode"]))
+    for k, ref in zip(SCALARS, z["scalars"]):
+        assert np.float32(out[k]) == np.float32(ref), (k, float(out[k]), float(ref))
+    assert out["N_pix_effective"] == pytest.approx(float(z["N_pix_effective"]), rel=1e-14)
+    for k in ARRAYS:
+        ref = z[f"out_{k}"]
+        got = np.asarray(out[k])
+        assert got.shape == ref.shape and got.dtype == ref.dtype, k
+        if ref.dtype == np.float32:
+            assert np.array_equal(got, ref), k
+        else:
+            scale = max(1e-300, float(np.abs(ref).max()))
+            assert np.abs(got - ref).max() <= 1e-14 * scale, k
+    for k in ("p00_POL", "p90_POL"):
+        for part, ref in ((0, z[f"out_{k}_r"]), (1, z[f"out_{k}_a"])):
+            assert np.array_equal(np.asarray(out[k][part]), ref), k
+
+
+def test_cases_cover_both_rho_modes_and_quiet_clusters():
+    z = [np.load(p) for p in CASES]
+    assert len(z) >= 6
+    assert any(bool(x["xgb_rho_mode"]) for x in z) and any(not bool(x["xgb_rho_mode"]) for x in z)
+    assert {int(x["n_ifo"]) for x in z} >= {2, 3, 4}
