@@ -352,6 +352,39 @@ int pgw_wdm_t2w(const double* ts, int64_t n_ts, int M, const double* filter, int
 /* Time slices of pgw_wdm_t2w: ceil(n_samples / M) (-1 for M < 1). */
 int64_t pgw_wdm_n_time(int64_t n_samples, int M);
 
+/* Statistics at the sky maximum of one cluster (SkyStatistics of
+ * sky_statistics.py:246-292, the scalars and the per-detector signal SNR). */
+typedef struct {
+  double N_pix_effective;
+  float Gn, Ec, Dc, Rc, Eh, Es, Np, Em, Lm, norm, cc, rho, xrho, Lo, Eo;
+  float S_snr[PGW_MAX_IFO];
+  int32_t status;   /* 0, PGW_ERR_DELAY_RANGE, or PGW_ERR_BAD_SHAPE for bad xtalk rows */
+  int32_t n_pix;
+  int32_t reserved;
+} pgw_skystat_result;
+
+/* Bytes of device workspace pgw_skystat_batched needs for total_pix pixels
+ * (0 for a bad n_ifo). */
+size_t pgw_skystat_workspace_bytes(int n_ifo, int64_t total_pix);
+
+/* compute_statistics_at_sky_position (sky_statistics.py:26-262) for every
+ * cluster of a lag in one launch, each at its own direction sky_idx[c]:
+ * cluster layout as in pgw_sky_loop_batched (pix_offsets n_clusters+1,
+ * td_offsets, rms_all (total_pix, n_ifo), td00_all/td90_all blocks (n_delay,
+ * n_ifo, P_c)); regulators[c] = the cluster's REG[1], REG0 = REG[0];
+ * xtalk: n_xtalk packed rows of 8 float32 (neighbour index within the
+ * cluster, 3 unused, 4 overlap coefficients), xtalk_lookup: per pixel the
+ * [start, end) row range (total_pix x 2 int64); ws: at least
+ * pgw_skystat_workspace_bytes.  One result per cluster; asynchronous. */
+int pgw_skystat_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
+                        const int64_t* td_offsets, int64_t total_pix, int64_t n_sky,
+                        const float* FP, const float* FX, const float* rms_all,
+                        const float* td00_all, const float* td90_all, int n_delay,
+                        const int32_t* ml, const int64_t* sky_idx, const float* regulators,
+                        float REG0, float network_energy_threshold, const float* xtalk,
+                        int64_t n_xtalk, const int64_t* xtalk_lookup, int xgb_rho_mode, void* ws,
+                        size_t ws_bytes, pgw_skystat_result* out, void* stream);
+
 /* Copy `bytes` from page-locked host memory (cudaHostAlloc'ed or registered)
  * to device memory with a kernel instead of the copy engine, asynchronously
  * on `stream`.  Input staging for the batched loop: the copy engine's first

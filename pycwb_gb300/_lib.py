@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
 SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu",
-           "wdm.cu"]
+           "wdm.cu", "skystat.cu"]
 HEADERS = ["common.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -121,6 +121,11 @@ def load():
         L.pgw_subnet_sky_batched.restype = ctypes.c_int
         L.pgw_sky_tables_healpix.argtypes = [i32, i32, P, P, f64, f64, i32, P, P, P, P]
         L.pgw_sky_tables_healpix.restype = ctypes.c_int
+        L.pgw_skystat_workspace_bytes.argtypes = [i32, i64]
+        L.pgw_skystat_workspace_bytes.restype = sz
+        L.pgw_skystat_batched.argtypes = [i32, i32, P, P, i64, i64, P, P, P, P, P, i32, P, P, P,
+                                          f32, f32, P, i64, P, i32, P, sz, P, P]
+        L.pgw_skystat_batched.restype = ctypes.c_int
         L.pgw_wdm_t2w.argtypes = [P, i64, i32, P, i64, P, P, P, P, i32, P]
         L.pgw_wdm_t2w.restype = ctypes.c_int
         L.pgw_wdm_n_time.argtypes = [i64, i32]

@@ -1,0 +1,111 @@
+"""Statistics at the sky maximum on the GPU (pgw_skystat_batched) against
+the reference's golden vectors and the oracle.
+
+The kernel rounds every float32 operation of the per-pixel pass as the
+reference does; its float64 sums run in pixel order where NumPy sums
+pairwise, and dpf's sum of f^4 squares twice where NumPy calls pow, so the
+statistics agree to rounding: |gpu - ref| <= 1e-4 max(|ref|, 1e-3 Em) +
+1e-6 (Em sets the energy scale of the differences Dc, Lm).
+"""
+
+import glob
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "skystat_*.npz")))
+SCALARS = ("Gn", "Ec", "Dc", "Rc", "Eh", "Es", "Np", "Em", "Lm", "norm", "cc", "rho", "xrho",
+           "Lo", "Eo")
+
+
+@pytest.fixture(scope="module")
+def ss():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pycwb_gb300 import _lib
+    _lib.build()
+    from pycwb_gb300.likelihoodWP import sky_statistics
+    return sky_statistics
+
+
+def _close(got, ref, em, what):
+    tol = 1e-4 * max(abs(ref), 1e-3 * abs(em)) + 1e-6
+    assert abs(got - ref) <= tol, (what, got, ref)
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_single_cluster_matches_reference(ss, path):
+    z = np.load(path)
+    n_ifo = int(z["n_ifo"])
+    got = ss.compute_statistics_at_sky_position(
+        int(z["sky_idx"]), n_ifo, int(z["n_pix"]), z["FP"], z["FX"], z["rms"], z["td00"],
+        z["td90"], z["ml"], z["REG"], float(z["network_energy_threshold"]), z["xtalk"],
+        z["xtalk_lookup"], xgb_rho_mode=bool(z["xgb_rho_mode"]))
+    ref = dict(zip(SCALARS, (float(v) for v in z["scalars"])))
+    for k in SCALARS:
+        _close(float(getattr(got, k)), ref[k], ref["Em"], k)
+    assert got.N_pix_effective == pytest.approx(float(z["N_pix_effective"]), rel=1e-6)
+    s_ref = z["out_S_snr"]
+    assert np.allclose(got.S_snr, s_ref, rtol=1e-5, atol=1e-7)
+
+
+def test_batched_matches_oracle(ss, oracle_mod):
+    from oracle import skystat_oracle
+    from pycwb_gb300 import sky
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch, SkyTables
+    from pycwb_gb300.synthetic import make_cluster, regulators
+    sys_path_golden = os.path.join(os.path.dirname(__file__), "golden")
+    import sys
+    sys.path.insert(0, sys_path_golden)
+    from make_golden import synthetic_xtalk
+
+    ifos = ["L1", "H1", "V1"]
+    rng = np.random.default_rng(7)
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(ifos, "L1", 512.0, 20, healpix_order=2)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    reg = regulators(3)
+    tables = SkyTables.from_arrays(FP_t, FX_t, ml, None, **{k: reg[k] for k in (
+        "network_energy_threshold", "gamma_regulator", "delta_regulator", "netCC")})
+    sizes = [40, 1, 25, 60, 7]
+    clusters, xts = [], []
+    for P in sizes:
+        td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, P, 20, float(rng.uniform(10, 40)))
+        clusters.append((td00, td90, rms))
+        xts.append(synthetic_xtalk(rng, P))
+    loop = BatchedSkyLoop(tables, ClusterBatch.from_clusters(clusters))
+    res = loop.run()
+    xt, lk = ss.pack_xtalk(xts)
+    out = ss.statistics_batched(loop, res.l_max, xt, lk)
+    assert out.shape == (len(sizes),) and np.all(out["status"] == 0)
+    REG0 = np.float32(reg["delta_regulator"] * math.sqrt(2))
+    for c, (td00, td90, rms) in enumerate(clusters):
+        REG = np.array([REG0, np.float32(res.regulator[c]), 0.0], np.float32)
+        ref = skystat_oracle.statistics_at_sky_position(
+            int(res.l_max[c]), 3, sizes[c], FP_t, FX_t, rms, td00, td90, ml, REG,
+            reg["network_energy_threshold"], xts[c][0], xts[c][1])
+        for k in SCALARS:
+            _close(float(out[k][c]), float(ref[k]), float(ref["Em"]), (c, k))
+        assert out["n_pix"][c] == sizes[c]
+
+
+def test_bad_xtalk_is_reported(ss):
+    z = np.load(CASES[0])
+    xt = np.array(z["xtalk"])
+    xt[3, 0] = 10_000                      # a neighbour outside the cluster
+    with pytest.raises(RuntimeError):
+        ss.compute_statistics_at_sky_position(
+            int(z["sky_idx"]), int(z["n_ifo"]), int(z["n_pix"]), z["FP"], z["FX"], z["rms"],
+            z["td00"], z["td90"], z["ml"], z["REG"], float(z["network_energy_threshold"]), xt,
+            z["xtalk_lookup"])
+    with pytest.raises(ValueError):
+        ss.compute_statistics_at_sky_position(
+            int(z["sky_idx"]), int(z["n_ifo"]), int(z["n_pix"]), z["FP"], z["FX"], z["rms"],
+            z["td00"], z["td90"], z["ml"], z["REG"], float(z["network_energy_threshold"]),
+            z["xtalk"], z["xtalk_lookup"][:-1])
