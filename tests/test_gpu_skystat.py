@@ -98,7 +98,11 @@ def test_batched_matches_oracle(ss, oracle_mod):
 def test_bad_xtalk_is_reported(ss):
     z = np.load(CASES[0])
     xt = np.array(z["xtalk"])
-    xt[3, 0] = 10_000                      # a neighbour outside the cluster
+    # a neighbour outside the cluster, in a row of the most active pixel (rows
+    # are read for pixels inside the event mask only, as in the reference)
+    i = int(np.argmax(z["out_pixel_mask"]))
+    assert z["out_pixel_mask"][i] > 0.5
+    xt[int(z["xtalk_lookup"][i][0]), 0] = 10_000
     with pytest.raises(RuntimeError):
         ss.compute_statistics_at_sky_position(
             int(z["sky_idx"]), int(z["n_ifo"]), int(z["n_pix"]), z["FP"], z["FX"], z["rms"],
