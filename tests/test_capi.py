@@ -68,3 +68,50 @@ def test_regulator_order_is_a_permutation():
     assert np.array_equal(np.sort(a), np.arange(valid.size))
     with pytest.raises(ValueError):
         _lib.regulator_order(FP_t, FX_t, np.array([0, FP_t.shape[0]], np.int64))
+
+
+def _struct_layout(struct, fields):
+    """sizeof and offsetof of a header struct, from a small host C program."""
+    import shutil
+    import subprocess
+    import tempfile
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    body = "".join(f'  printf("%zu\\n", offsetof({struct}, {f}));\n' for f in fields)
+    src = ("#include <stddef.h>\n#include <stdio.h>\n#include <stdint.h>\n"
+           "typedef void* cudaStream_t;\n"
+           f'#include "{HEADER}"\n'
+           f'int main(void) {{\n  printf("%zu\\n", sizeof({struct}));\n{body}  return 0;\n}}\n')
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "layout.c")
+        exe = os.path.join(d, "layout")
+        open(c, "w").write(src)
+        subprocess.run([cc, "-std=c11", "-o", exe, c], check=True, capture_output=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    return int(out[0]), [int(x) for x in out[1:]]
+
+
+def test_result_structs_match_the_python_dtypes():
+    """The header's result structs and the numpy dtypes the Python layer reads
+    them with agree field by field."""
+    from pycwb_gb300._device import RESULT_DTYPE
+    from pycwb_gb300.likelihoodWP.sky_statistics import SKYSTAT_DTYPE
+    from pycwb_gb300.super_cluster.sub_net_cut import SUBNET_DTYPE
+    for struct, dt in (("pgw_skystat_result", SKYSTAT_DTYPE), ("pgw_subnet_result", SUBNET_DTYPE),
+                       ("pgw_scan_result", RESULT_DTYPE)):
+        names = list(dt.names)
+        size, offs = _struct_layout(struct, names)
+        assert size == dt.itemsize, struct
+        assert offs == [dt.fields[n][1] for n in names], struct
+
+
+def test_pack_xtalk_offsets_rows():
+    import numpy as np
+    from pycwb_gb300.likelihoodWP.sky_statistics import pack_xtalk
+    a = (np.arange(16, dtype=np.float32).reshape(2, 8), np.array([[0, 1], [1, 2]]))
+    b = (np.ones((3, 8), np.float32), np.array([[0, 3]]))
+    xt, lk = pack_xtalk([a, b])
+    assert xt.shape == (5, 8) and lk.tolist() == [[0, 1], [1, 2], [2, 5]]
+    xt0, lk0 = pack_xtalk([])
+    assert xt0.shape == (0, 8) and lk0.shape == (0, 2)
