@@ -55,3 +55,29 @@ def test_cases_cover_both_rho_modes_and_quiet_clusters():
     assert len(z) >= 6
     assert any(bool(x["xgb_rho_mode"]) for x in z) and any(not bool(x["xgb_rho_mode"]) for x in z)
     assert {int(x["n_ifo"]) for x in z} >= {2, 3, 4}
+
+
+def test_packet_helpers_known_answers(oracle_mod):
+    """The reference's own known-answer tests of the packet helpers
+    (pycwb/modules/likelihoodWP/tests/test_packet_ops_contract.py:37-121),
+    applied to the oracle's restatements."""
+    from oracle import skystat_oracle as so
+    # null packet: plain float32 differences (:37-50)
+    d = np.array([[1.0, 2.0], [3.0, 4.0]], np.float32)
+    h = np.array([[0.5, 1.0], [1.5, 2.0]], np.float32)
+    assert np.array_equal(np.asarray(d, np.float32) - np.asarray(h, np.float32), d - h)
+    # xtalk energy: an active pixel without neighbours contributes nothing (:53-70)
+    p = np.array([[1.0, 0.5]])
+    q = np.array([[2.0, 1.0]])
+    assert so.xtalk_energy(p, q, np.zeros((0, 8)), np.array([[0, 0], [0, 0]]),
+                           np.array([1.0, 0.0])) == 0.0
+    # packet norms with every pixel masked: norms clamp at 2, SNR = q_E (:73-93)
+    snr, norm, rn, qn = so.packet_norm(np.array([[1.0, 2.0]], np.float32),
+                                       np.array([[3.0, 4.0]], np.float32), np.zeros((0, 8)),
+                                       np.array([[0, 0], [0, 0]]), np.array([0.0, 0.0], np.float32),
+                                       np.array([5.0], np.float32))
+    assert np.allclose(snr, [5.0]) and np.all(norm == 2.0) and not rn.any() and not qn.any()
+    # signal norms (:96-112): 2 p_E / q_E, the data norms kept
+    q_E, p_E = np.array([4.0]), np.array([3.0], np.float32)
+    s_snr = (p_E * 2) / q_E
+    assert s_snr.sum() == pytest.approx(1.5)
