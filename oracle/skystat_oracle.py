@@ -155,6 +155,19 @@ def xtalk_energy(p, q, xt, lookup, msk):
     return float(np.sum(g))
 
 
+def signal_norms(q_norm, q_E, p_E, ec):
+    """gw_norm_numpy (packet_ops.py:905-948): (total SNR, per-detector SNR
+    2 p_E / q_E, the data norms q_E, the signal pixel norms)."""
+    snr = (np.asarray(p_E) * 2) / np.asarray(q_E, np.float64)
+    p_norm = np.where(np.asarray(ec)[None, :] > 0, q_norm, 0.0)
+    return float(np.sum(snr)), snr, np.asarray(q_E, np.float64).copy(), p_norm
+
+
+def null_packet(d, D, h, H):
+    """avx_loadNULL_ps (packet_ops.py:333-361): data minus signal, float32."""
+    return (np.asarray(d, F32) - np.asarray(h, F32), np.asarray(D, F32) - np.asarray(H, F32))
+
+
 def noise_correction(p_norm, q_norm, et, msk, ec, gn, rn):
     """avx_noise_ps (packet_ops.py:93-231); gn is updated in place."""
     I = p_norm.shape[0]
@@ -219,15 +232,12 @@ def statistics_at_sky_position(sky_idx, n_ifo, n_pix, FP, FX, rms, td00, td90, m
     Eo, pd, pD, E_d, si_d, co_d, a_d, A_d = packet(d["v0"], d["v9"], msk)
     Lo, ps, pS, E_s, si_s, co_s, a_s, A_s = packet(d["s"], d["S"], msk)
     _, norm_d, rn_x, qn_d = packet_norm(pd, pD, xtalk, xtalk_lookup, msk, E_d)
-    # gw_norm_numpy (packet_ops.py:905-948)
-    s_snr = (E_s * 2) / norm_d
-    p_norm = np.where(ec[None, :] > 0, qn_d, 0.0)
+    _, s_snr, _, p_norm = signal_norms(qn_d, norm_d, E_s, ec)
     Gn, Ec, Dc, Rc, Eh, Es, NC, NS = noise_correction(p_norm, qn_d, et, msk, ec, gn, rn_x)
     N_eff, pd, pD = set_amplitudes(pd, pD, qn_d, si_d, co_d, a_d, A_d, msk)
     N_eff = N_eff - 1
     _, ps, pS = set_amplitudes(ps, pS, p_norm, si_s, co_s, a_s, A_s, msk)
-    n00 = np.asarray(pd, F32) - np.asarray(ps, F32)
-    n90 = np.asarray(pD, F32) - np.asarray(pS, F32)
+    n00, n90 = null_packet(pd, pD, ps, pS)
     Em = xtalk_energy(pd, pD, xtalk, xtalk_lookup, msk)
     Np = xtalk_energy(n00, n90, xtalk, xtalk_lookup, msk)
     Lm = Em - Np - Gn

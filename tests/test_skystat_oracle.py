@@ -64,8 +64,11 @@ def test_packet_helpers_known_answers(oracle_mod):
     from oracle import skystat_oracle as so
     # null packet: plain float32 differences (:37-50)
     d = np.array([[1.0, 2.0], [3.0, 4.0]], np.float32)
+    D = np.array([[5.0, 6.0], [7.0, 8.0]], np.float32)
     h = np.array([[0.5, 1.0], [1.5, 2.0]], np.float32)
-    assert np.array_equal(np.asarray(d, np.float32) - np.asarray(h, np.float32), d - h)
+    H = np.array([[2.5, 3.0], [3.5, 4.0]], np.float32)
+    n, N = so.null_packet(d, D, h, H)
+    assert np.array_equal(n, d - h) and np.array_equal(N, D - H)
     # xtalk energy: an active pixel without neighbours contributes nothing (:53-70)
     p = np.array([[1.0, 0.5]])
     q = np.array([[2.0, 1.0]])
@@ -78,6 +81,7 @@ def test_packet_helpers_known_answers(oracle_mod):
                                        np.array([5.0], np.float32))
     assert np.allclose(snr, [5.0]) and np.all(norm == 2.0) and not rn.any() and not qn.any()
     # signal norms (:96-112): 2 p_E / q_E, the data norms kept
-    q_E, p_E = np.array([4.0]), np.array([3.0], np.float32)
-    s_snr = (p_E * 2) / q_E
-    assert s_snr.sum() == pytest.approx(1.5)
+    total, snr, kept, p_norm = so.signal_norms(np.array([[0.5, 0.3]]), np.array([4.0]),
+                                               np.array([3.0]), np.array([0.1, 0.0]))
+    assert total > 0 and total == pytest.approx(1.5) and kept[0] == 4.0
+    assert p_norm.tolist() == [[0.5, 0.0]]
