@@ -147,3 +147,33 @@ def test_rms_normalisation_and_layout():
     with pytest.raises(ValueError):
         load_data_from_pixels(None, 4, pixel_arrays=pa)
     _ = _extract_pixel_array_time_delay_data(pa)
+
+
+def test_sky_mask_reference_cases():
+    """The cases of the reference's own sky-mask tests
+    (pycwb/modules/likelihoodWP/tests/test_compute_sky_valid_indices.py:
+    None and UniformAllSky configs, a legacy Patch in radians and degrees, a
+    zero radius on a grid point, the full sky) on a 300-direction spiral."""
+    n = 300
+    k = np.arange(n, dtype=np.float64)
+    phi = (np.pi * (3.0 - np.sqrt(5.0)) * k) % (2.0 * np.pi)
+    lat = np.arcsin(np.clip(1.0 - 2.0 * (k + 0.5) / n, -1.0, 1.0))
+    assert np.array_equal(compute_sky_valid_indices(phi, lat, None), np.arange(n))
+    assert compute_sky_valid_indices(phi, lat, None).dtype == np.int64
+    assert compute_sky_valid_indices(np.array([1.0]), np.array([0.5]), None).tolist() == [0]
+    rad = {"type": "Patch", "patch": {"center": {"phi": 1.0, "theta": 0.3}, "radius": 0.5,
+                                      "unit": "rad"}}
+    deg = {"type": "Patch", "patch": {"center": {"phi": math.degrees(1.0),
+                                                 "theta": math.degrees(0.3)},
+                                      "radius": math.degrees(0.5), "unit": "deg"}}
+    v = compute_sky_valid_indices(phi, lat, rad)
+    sep = np.arccos(np.clip(np.sin(lat) * math.sin(0.3) + np.cos(lat) * math.cos(0.3)
+                            * np.cos(phi - 1.0), -1.0, 1.0))
+    assert np.array_equal(v, np.flatnonzero(sep <= 0.5)) and v.size > 0
+    assert np.array_equal(compute_sky_valid_indices(phi, lat, deg), v)
+    zero = {"type": "Patch", "patch": {"center": {"phi": float(phi[5]), "theta": float(lat[5])},
+                                       "radius": 0.0, "unit": "rad"}}
+    assert compute_sky_valid_indices(phi, lat, zero).tolist() == [5]
+    full = {"type": "Patch", "patch": {"center": {"phi": 1.0, "theta": 0.3}, "radius": math.pi,
+                                       "unit": "rad"}}
+    assert compute_sky_valid_indices(phi, lat, full).size == n
