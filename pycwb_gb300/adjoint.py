@@ -134,7 +134,7 @@ def refine(inp: GradInputs, l_max, grid_theta, grid_phi, grid_stat, n_steps=10,
     """Off-grid refinement of each cluster's grid maximum.
 
     Gradient ascent on the continuous statistic starts at the grid maximum
-    l_max.  The grid result is the fallback and the judge: the refined
+    l_max.  The grid result is the fallback and the arbiter: the refined
     direction is kept only if its statistic beats the continuous statistic
     at the grid direction and it lies within `max_cells` grid spacings of
     it; otherwise the grid direction is returned.  The grid scan's
