@@ -115,3 +115,18 @@ def test_pack_xtalk_offsets_rows():
     assert xt.shape == (5, 8) and lk.tolist() == [[0, 1], [1, 2], [2, 5]]
     xt0, lk0 = pack_xtalk([])
     assert xt0.shape == (0, 8) and lk0.shape == (0, 2)
+
+
+def test_skystat_workspace_size_is_pure_host_arithmetic():
+    from pycwb_gb300 import _lib
+    try:
+        _lib.build()
+    except (RuntimeError, FileNotFoundError) as e:
+        pytest.skip(f"nvcc unavailable: {e}")
+    L = _lib.load()
+    a = L.pgw_skystat_workspace_bytes(3, 1000)
+    assert a >= 1000 * ((10 * 3 + 6) * 4 + (8 * 3 + 1) * 8)
+    assert L.pgw_skystat_workspace_bytes(3, 2000) > a
+    assert L.pgw_skystat_workspace_bytes(3, 0) > 0
+    assert L.pgw_skystat_workspace_bytes(0, 10) == 0 and L.pgw_skystat_workspace_bytes(9, 10) == 0
+    assert L.pgw_wdm_n_time(1000, 16) == 63 and L.pgw_wdm_n_time(10, 0) == -1
