@@ -65,3 +65,18 @@ def test_delay_table_sign_and_reference_row():
     anti = np.argmax(n @ (-n).T, axis=1)
     assert np.allclose(n[anti], -n, atol=1e-12)
     assert np.array_equal(ml[1][anti], -ml[1])
+
+
+def test_baseline_and_response_known_answers():
+    """pycwb/types/tests/test_detector_geometry.py:209-225, 680-683: the
+    H1-L1 light travel time is 10.013 ms, vertices sit at the Earth's
+    radius, response tensors are symmetric and traceless (two orthogonal
+    unit arms, (x x^T - y y^T) / 2)."""
+    h1, l1 = sky.DetectorSite("H1"), sky.DetectorSite("L1")
+    assert np.linalg.norm(h1.vertex - l1.vertex) / sky.C_LIGHT == pytest.approx(0.010013,
+                                                                                 rel=1e-4)
+    for d in ("H1", "L1", "V1", "K1"):
+        site = sky.DetectorSite(d)
+        assert 6.3e6 < np.linalg.norm(site.vertex) < 6.4e6
+        assert np.allclose(site.response, site.response.T)
+        assert abs(np.trace(site.response)) < 1e-12
