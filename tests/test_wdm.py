@@ -177,3 +177,20 @@ def test_errors():
         wdm.WDM(16, 16).td_inputs(np.zeros(10_000))     # no TD filters yet
     with pytest.raises(ValueError):
         wdm.edge_series("cos", 9)
+
+
+@pytest.mark.parametrize("M,m0", [(16, 5), (32, 20), (8, 1)])
+def test_layer_m_holds_frequency_m_df(M, m0):
+    """Layer m covers the band around m * rate / (2M) (df = rate / 2M): a
+    sinusoid at that frequency puts nearly all of its energy in layer m, and
+    the 00 and 90 maps share it evenly."""
+    rate = 512.0
+    n = 8192
+    t = np.arange(n) / rate
+    x = np.sin(2 * np.pi * m0 * rate / (2 * M) * t + 0.3)
+    w = wdm.WDM(M, M, 4, 10)
+    a00, a90 = wdm_oracle.t2w(x, M, w.filter)
+    inner = slice(a00.shape[0] // 4, 3 * a00.shape[0] // 4)
+    e = (a00[inner] ** 2 + a90[inner] ** 2).sum(axis=0)
+    assert e[m0] / e.sum() > 0.99
+    assert (a00[inner, m0] ** 2).sum() == pytest.approx((a90[inner, m0] ** 2).sum(), rel=0.05)
