@@ -192,6 +192,74 @@ def cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=32, n_dirs=2048, seed=7, t
     return time.perf_counter() - t0, pairs, evals, idx
 
 
+def parity_sample(res, batch, ml, FP_t, FX_t, reg, order, n_dirs=2000, seed=11):
+    """The oracle against the GPU's own results on three clusters of the timed
+    batch (the smallest, the median and the largest), outside the timed region.
+
+    Per cluster: REG[1] over the whole sky must equal the oracle's; the 11 maps
+    at n_dirs random directions plus the 25 directions nearest the GPU's
+    maximum are compared under the parity tolerance (1e-4 relative, floor
+    1e-3 of the map's largest value, plus twice the reference's own float32
+    error against float64); the oracle's maximum over that sample must be the
+    GPU's (or tie within 1e-5)."""
+    from oracle import oracle
+    from pycwb_gb300 import sky
+
+    oracle.build()
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(seed)
+    n_sky = ml.shape[1]
+    phi, lat = sky.build_sky_directions(n_sky, healpix_order=order)
+    xyz = np.stack([np.cos(lat) * np.cos(phi), np.cos(lat) * np.sin(phi), np.sin(lat)], axis=1)
+    srt = np.argsort(batch.sizes, kind="stable")
+    picks = [int(srt[0]), int(srt[srt.size // 2]), int(srt[-1])]
+    full = np.arange(n_sky, dtype=np.int64)
+    REG0 = np.float32(reg["delta_regulator"] * math.sqrt(2))
+    rows = []
+    for c in picks:
+        td00, td90, rms = batch.cluster_views(c)
+        reg1 = oracle.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
+                                    reg["network_energy_threshold"], full)
+        lg = int(res.l_max[c])
+        near = np.argsort(-(xyz @ xyz[lg]), kind="stable")[:25]
+        sub = np.unique(np.concatenate([rng.choice(n_sky, n_dirs, replace=False), near]))
+        sub = sub.astype(np.int64)
+        REG = np.array([REG0, reg1, 0.0], np.float32)
+        args = (3, rms.shape[0], n_sky, FP_t, FX_t, rms, td00, td90, ml)
+        tail = (reg["netCC"], reg["delta_regulator"], reg["network_energy_threshold"], sub)
+        ref = oracle.scan_sky_for_best_fit(*args, REG, *tail)
+        f64 = oracle.scan_sky_for_best_fit(*args, REG.astype(np.float64), *tail, precision="f64")
+        maps = res.maps[c][:, torch_index(sub, res.maps.device)].cpu().numpy().astype(np.float64)
+        worst = 0.0
+        for k in range(11):
+            a, b, d = maps[k], ref[k + 1][sub].astype(np.float64), f64[k + 1][sub]
+            ok = ~(np.isnan(a) | np.isnan(b))
+            if not ok.any():
+                continue
+            den = np.maximum(np.abs(b[ok]), 1e-3 * max(np.max(np.abs(b[ok])), 1e-30))
+            diff = np.maximum(np.abs(a[ok] - b[ok]) - 2.0 * np.nan_to_num(np.abs(b[ok] - d[ok])), 0)
+            worst = max(worst, float(np.max(diff / den)))
+        lr = int(ref[0])
+        tie = lr != lg and abs(float(ref[7][lr]) - float(ref[7][lg])) <= 1e-5 * abs(float(ref[7][lr]))
+        rows.append({"cluster": c, "pixels": int(rms.shape[0]),
+                     "regulator_equal": bool(np.float32(res.regulator[c]) == np.float32(reg1)),
+                     "l_max_equal": lr == lg, "near_tie": bool(tie),
+                     "max_rel_err": worst, "directions": int(sub.size)})
+    return {"clusters": rows,
+            "all_pass": all(r["regulator_equal"] and (r["l_max_equal"] or r["near_tie"])
+                            and r["max_rel_err"] <= 1e-4 for r in rows),
+            "seconds": round(time.perf_counter() - t0, 1),
+            "rule": "REG[1] equal over the whole sky; maps within 1e-4 relative (floor 1e-3 of "
+                    "the map's max, plus 2x the reference's float32 error vs float64) at "
+                    f"{n_dirs} random directions + the 25 nearest the GPU maximum; oracle "
+                    "maximum over that sample = GPU maximum or a tie within 1e-5"}
+
+
+def torch_index(idx, device):
+    import torch
+    return torch.from_numpy(np.asarray(idx, np.int64)).to(device)
+
+
 def cpu_rate(batch, ml, FP_t, FX_t, reg, target_s=12.0):
     """Cluster-sky evals/s of the oracle on all host cores, normalised to the
     workload's mean cluster size (evals/s = pairs/s / mean pixels)."""
@@ -223,6 +291,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle comparison on three clusters of the timed batch")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-td", action="store_true")
@@ -466,6 +536,10 @@ def main():
         plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
         plain["roofline_frac"] = (useful_ops / (plain["ms"] * 1e-3) / 1e12 / peak) if peak else None
 
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = parity_sample(res, batch, ml, FP_t, FX_t, reg, args.order)
+
     adjoint = time_adjoint(loop, res, batch, args.order, dev) if not args.no_adjoint else None
     td_build = time_td_build(dev) if not args.no_td else None
     wdm_field = time_wdm(dev) if not args.no_wdm else None
@@ -522,6 +596,7 @@ def main():
             "wdm": wdm_field,
             "pipeline": pipeline,
             "subnet": subnet,
+            "parity_sample": parity,
             "selected": {"found": int(found.sum()),
                          "l_max_equals_injected": int(np.sum(l_max == l_true))},
             "step_ms": step_ms,

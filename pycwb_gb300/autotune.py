@@ -25,7 +25,8 @@ from . import _lib
 
 CACHE_PATH = os.environ.get(
     "PYCWB_GB300_TUNE_CACHE",
-    os.path.join(os.path.dirname(os.path.abspath(__file__)), ".tile_shapes.json"))
+    os.path.join(os.environ.get("XDG_CACHE_HOME", os.path.join(os.path.expanduser("~"), ".cache")),
+                 "pycwb_gb300", "tile_shapes.json"))
 _lock = threading.Lock()
 
 
@@ -58,6 +59,10 @@ def _store(key, shape, timings):
     with _lock:
         cache = _load_cache()
         cache[key] = {"shape": list(shape.key()), "timings_ms": timings}
+        try:
+            os.makedirs(os.path.dirname(CACHE_PATH), exist_ok=True)
+        except OSError:
+            return                     # no writable cache: the shape is re-measured next time
         tmp = CACHE_PATH + ".tmp"
         with open(tmp, "w") as f:
             json.dump(cache, f, indent=1)

@@ -274,6 +274,12 @@ class BatchedSkyLoop:
         r = self.res_host.numpy().view(dv.RESULT_DTYPE).reshape(-1)
         status = int(np.bitwise_or.reduce(r["status"])) if r.size else 0
         _lib.check_device_status(status, "sky_loop_batched")
+        # the maps were allocated on the loop's stream and are read on the
+        # caller's: keep the caching allocator from handing their memory to
+        # new work on the loop's stream before the caller's queued reads ran
+        cur = torch.cuda.current_stream(self.stats.device)
+        if cur != self.stream:
+            self.stats.record_stream(cur)
         return BatchResult(l_max=r["l_max"].copy(), sky_stat_max=r["sky_stat_max"].copy(),
                            found=r["found"].astype(bool), regulator=self.regs_host.numpy().copy(),
                            maps=self.stats, active_pairs=r["active_pairs"].copy())
