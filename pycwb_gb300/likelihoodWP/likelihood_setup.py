@@ -11,94 +11,19 @@ device is given.  Constants (likelihood_setup.py:133-147):
     net_rho_threshold        = |netRHO|
     netEC_threshold          = 2 netRHO^2
 
-Sky masks (pycwb/modules/likelihoodWP/sky_mask.py:71-176): UniformAllSky,
-and Patch / Fixed in Earth-fixed coordinates ("geo": longitude/latitude;
-"cwb": phi_geo/theta_cwb, co-latitude) with angles as "<value> deg" or
-"<value> rad" strings, or numbers in radians.  ICRS masks (a GPS-time
-sidereal rotation) and Custom HEALPix-map masks are not supported and
-raise NotImplementedError.
+Sky masks: ``sky_mask.compute_sky_valid_indices`` (UniformAllSky, Patch,
+Fixed and Custom HEALPix maps in geo, cwb or ICRS coordinates), evaluated
+at the segment start; ICRS masks are evaluated again per cluster at the
+cluster's time by ``sky_mask.sky_valid_indices_for_cluster``.
 """
 
 from __future__ import annotations
-
-import math
 
 import numpy as np
 
 from .. import sky
 from .pixel_data import build_sky_delay_and_antenna_patterns
-
-_COORD_KEYS = {"geo": ("longitude", "latitude"), "cwb": ("phi_geo", "theta_cwb")}
-
-
-def _angle(v, name: str) -> float:
-    """Radians from a number (radians) or a '<value> deg|rad' string."""
-    if isinstance(v, str):
-        parts = v.split()
-        if len(parts) != 2 or parts[1] not in ("deg", "rad"):
-            raise ValueError(f"{name} must be '<value> deg' or '<value> rad', got {v!r}")
-        x = float(parts[0])
-        return math.radians(x) if parts[1] == "deg" else x
-    return float(v)
-
-
-def _earth_fixed(values, coordsys: str, context: str, legacy_unit=None):
-    """(phi_geo, latitude) radians of a mask point."""
-    if coordsys not in _COORD_KEYS:
-        raise NotImplementedError(f"{context}: coordsys {coordsys!r} needs the sidereal rotation "
-                                  "of the event time; only 'geo' and 'cwb' are supported")
-    a, b = _COORD_KEYS[coordsys]
-    if a in values and b in values:
-        first, second = _angle(values[a], f"{context}.{a}"), _angle(values[b], f"{context}.{b}")
-    elif "phi" in values and "theta" in values:
-        scale = math.pi / 180.0 if legacy_unit == "deg" else 1.0
-        first, second = float(values["phi"]) * scale, float(values["theta"]) * scale
-    else:
-        raise ValueError(f"{context} needs keys {a!r} and {b!r}")
-    if coordsys == "geo":
-        if not -math.pi / 2 <= second <= math.pi / 2:
-            raise ValueError(f"{context}.latitude must be within [-90 deg, 90 deg]")
-        return first % (2 * math.pi), second
-    if not 0.0 <= second <= math.pi:
-        raise ValueError(f"{context}.theta_cwb must be within [0 deg, 180 deg]")
-    return first % (2 * math.pi), math.pi / 2 - second
-
-
-def compute_sky_valid_indices(phi_geo_arr, latitude_arr, sky_mask_config, t_ref=None):
-    """Sorted int64 indices of the directions the mask keeps (sky_mask.py:71-176)."""
-    phi = np.asarray(phi_geo_arr, np.float64)
-    lat = np.asarray(latitude_arr, np.float64)
-    if phi.shape != lat.shape:
-        raise ValueError("Sky longitude and latitude arrays must have identical shapes")
-    n_sky = phi.size
-    if not sky_mask_config or sky_mask_config.get("type", "UniformAllSky") == "UniformAllSky":
-        return np.arange(n_sky, dtype=np.int64)
-    kind = sky_mask_config["type"]
-    coordsys = str(sky_mask_config.get("coordsys", "geo")).lower()
-    if kind == "Patch":
-        patch = sky_mask_config["patch"]
-        unit = patch.get("unit", "rad")
-        c_phi, c_lat = _earth_fixed(patch["center"], coordsys, "sky_mask.patch.center", unit)
-        r = patch["radius"]
-        radius = _angle(r, "sky_mask.patch.radius") if isinstance(r, str) else \
-            float(r) * (math.pi / 180.0 if unit == "deg" else 1.0)
-        if not 0.0 <= radius <= math.pi:
-            raise ValueError("sky_mask.patch.radius must be within [0 deg, 180 deg]")
-        cos_d = np.sin(lat) * math.sin(c_lat) + np.cos(lat) * math.cos(c_lat) * np.cos(phi - c_phi)
-        return np.where(np.arccos(np.clip(cos_d, -1.0, 1.0)) <= radius)[0].astype(np.int64)
-    if kind == "Fixed":
-        coords = sky_mask_config["coordinates"]
-        coords = coords.get("sky_loc", coords)
-        f_phi, f_lat = _earth_fixed(coords, coordsys, "sky_mask.coordinates",
-                                    sky_mask_config["coordinates"].get("unit", "rad"))
-        if n_sky == 0:
-            return np.array([], dtype=np.int64)
-        cos_d = np.sin(lat) * math.sin(f_lat) + np.cos(lat) * math.cos(f_lat) * np.cos(phi - f_phi)
-        return np.array([int(np.argmax(np.clip(cos_d, -1.0, 1.0)))], dtype=np.int64)
-    if kind == "Custom":
-        raise NotImplementedError("Custom HEALPix-map sky masks need healpy's map reader")
-    raise ValueError(f"Unknown sky_mask type: {kind!r}; supported types are "
-                     "UniformAllSky, Patch, Fixed, Custom")
+from .sky_mask import compute_sky_valid_indices, sky_valid_indices_for_cluster  # noqa: F401
 
 
 def prepare_likelihood_inputs(config, strains, nIFO, ml=None, FP=None, FX=None, ml_big=None,

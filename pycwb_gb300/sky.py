@@ -90,6 +90,112 @@ def healpix_pix2ang_ring(nside: int, ipix: np.ndarray):
     return theta, phi
 
 
+def _zphi(theta, phi):
+    theta = np.asarray(theta, dtype=np.float64)
+    phi = np.asarray(phi, dtype=np.float64)
+    if theta.shape != phi.shape:
+        theta, phi = np.broadcast_arrays(theta, phi)
+    if np.any((theta < 0.0) | (theta > math.pi)):
+        raise ValueError("theta must lie in [0, pi]")
+    z = np.cos(theta)
+    tt = np.mod(phi, 2.0 * math.pi) * (2.0 / math.pi)   # in [0, 4)
+    tt = np.where(tt >= 4.0, 0.0, tt)
+    return z, np.abs(z), tt
+
+
+def healpix_ang2pix_ring(nside: int, theta, phi) -> np.ndarray:
+    """RING-scheme pixel holding each direction (theta co-latitude, phi
+    longitude, radians), by the published scheme (Gorski et al. 2005,
+    section 4): in the equatorial belt |z| <= 2/3 the ring and the position
+    along it follow from the two families of pixel-boundary lines
+    j+ = nside (1/2 + t - 3z/4) and j- = nside (1/2 + t + 3z/4) (t = 2 phi / pi);
+    in the polar caps from the same lines scaled by sqrt(3 (1 - |z|))."""
+    nside = int(nside)
+    z, za, tt = _zphi(theta, phi)
+    out = np.empty(z.shape, dtype=np.int64)
+    npix = 12 * nside * nside
+    ncap = 2 * nside * (nside - 1)
+    eq = za <= 2.0 / 3.0
+    if np.any(eq):
+        t1 = nside * (0.5 + tt[eq])
+        t2 = nside * z[eq] * 0.75
+        jp = (t1 - t2).astype(np.int64)
+        jm = (t1 + t2).astype(np.int64)
+        ir = nside + 1 + jp - jm                      # ring counted from z = 2/3, 1..2 nside+1
+        kshift = 1 - (ir & 1)
+        ip = (jp + jm - nside + kshift + 1) // 2
+        ip = np.mod(ip, 4 * nside)
+        out[eq] = ncap + (ir - 1) * 4 * nside + ip
+    pol = ~eq
+    if np.any(pol):
+        t = tt[pol]
+        tp = t - np.floor(t)
+        tmp = nside * np.sqrt(3.0 * (1.0 - za[pol]))
+        jp = (tp * tmp).astype(np.int64)
+        jm = ((1.0 - tp) * tmp).astype(np.int64)
+        ir = jp + jm + 1                              # ring counted from the nearer pole
+        ip = (t * ir).astype(np.int64)
+        ip = np.mod(ip, 4 * ir)
+        north = z[pol] > 0
+        out[pol] = np.where(north, 2 * ir * (ir - 1) + ip, npix - 2 * ir * (ir + 1) + ip)
+    return out
+
+
+def _spread_bits(v: np.ndarray) -> np.ndarray:
+    """Bit k of v moved to bit 2k (v < 2^29)."""
+    v = v.astype(np.uint64)
+    out = np.zeros(v.shape, dtype=np.uint64)
+    for k in range(29):
+        out |= ((v >> np.uint64(k)) & np.uint64(1)) << np.uint64(2 * k)
+    return out
+
+
+def healpix_ang2pix_nest(nside: int, theta, phi) -> np.ndarray:
+    """NESTED-scheme pixel holding each direction: the base face (0-3 north,
+    4-7 equatorial, 8-11 south) from the same boundary lines as the RING
+    scheme, then the pixel's (x, y) within the face with the bits of x and y
+    interleaved (Gorski et al. 2005, section 4)."""
+    nside = int(nside)
+    if nside < 1 or nside & (nside - 1):
+        raise ValueError("nside must be a power of two for the NESTED scheme")
+    z, za, tt = _zphi(theta, phi)
+    face = np.empty(z.shape, dtype=np.int64)
+    ix = np.empty(z.shape, dtype=np.int64)
+    iy = np.empty(z.shape, dtype=np.int64)
+    eq = za <= 2.0 / 3.0
+    if np.any(eq):
+        t1 = nside * (0.5 + tt[eq])
+        t2 = nside * (z[eq] * 0.75)
+        jp = (t1 - t2).astype(np.int64)
+        jm = (t1 + t2).astype(np.int64)
+        ifp = jp // nside
+        ifm = jm // nside
+        face[eq] = np.where(ifp == ifm, ifp | 4, np.where(ifp < ifm, ifp, ifm + 8))
+        ix[eq] = jm & (nside - 1)
+        iy[eq] = nside - (jp & (nside - 1)) - 1
+    pol = ~eq
+    if np.any(pol):
+        t = tt[pol]
+        ntt = np.minimum(3, t.astype(np.int64))
+        tp = t - ntt
+        tmp = nside * np.sqrt(3.0 * (1.0 - za[pol]))
+        jp = np.minimum((tp * tmp).astype(np.int64), nside - 1)
+        jm = np.minimum(((1.0 - tp) * tmp).astype(np.int64), nside - 1)
+        north = z[pol] >= 0
+        face[pol] = np.where(north, ntt, ntt + 8)
+        ix[pol] = np.where(north, nside - jm - 1, jp)
+        iy[pol] = np.where(north, nside - jp - 1, jm)
+    xy = _spread_bits(ix) | (_spread_bits(iy) << np.uint64(1))
+    return face * nside * nside + xy.astype(np.int64)
+
+
+def healpix_ring_to_nest(nside: int) -> np.ndarray:
+    """NESTED index of every RING pixel (ring index order)."""
+    nside = int(nside)
+    theta, phi = healpix_pix2ang_ring(nside, np.arange(12 * nside * nside))
+    return healpix_ang2pix_nest(nside, theta, phi)
+
+
 def _isqrt(v: np.ndarray) -> np.ndarray:
     r = np.floor(np.sqrt(v.astype(np.float64))).astype(np.int64)
     # exact integer correction of the float estimate
