@@ -385,6 +385,24 @@ int pgw_skystat_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                         int64_t n_xtalk, const int64_t* xtalk_lookup, int xgb_rho_mode, void* ws,
                         size_t ws_bytes, pgw_skystat_result* out, void* stream);
 
+/* Normalised sky probability of selected clusters of a batched sky loop:
+ * the reference caller's softmax of the sky-statistic map
+ * (pycwb/modules/likelihoodWP/likelihood.py:338-342: p = exp(s - max s) /
+ * sum exp(s - max s) over all n_sky entries, float64 arithmetic, float32
+ * result), computed where the maps already are.  stats: the loop's
+ * out_stats, cluster c's (11, n_sky) block at c * stats_stride floats;
+ * clusters: n_select cluster indices (device int32), or NULL for clusters
+ * 0..n_select-1; out_probability: (n_select, n_sky) float32.  out_summary
+ * (may be NULL): per selected cluster 4 float64 -- max s, sum exp(s - max s),
+ * and the number of directions, largest probability first, holding 50 % and
+ * 90 % of the probability (inputs of an error region; the reference's
+ * compute_sky_error_region, detection_statistics.py:520-534, is a
+ * placeholder).  A NaN anywhere in a map makes its probabilities NaN, as in
+ * NumPy.  Asynchronous on `stream`; allocates nothing. */
+int pgw_sky_probability(int n_select, int64_t n_sky, const float* stats, int64_t stats_stride,
+                        const int32_t* clusters, float* out_probability, double* out_summary,
+                        void* stream);
+
 /* Copy `bytes` from page-locked host memory (cudaHostAlloc'ed or registered)
  * to device memory with a kernel instead of the copy engine, asynchronously
  * on `stream`.  Input staging for the batched loop: the copy engine's first

@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
 SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu",
-           "wdm.cu", "skystat.cu"]
+           "wdm.cu", "skystat.cu", "skyprob.cu"]
 HEADERS = ["common.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -138,6 +138,8 @@ def load():
                                            f64, P, i64, P, P, P, P, P]
         L.pgw_sky_loop_noalloc.restype = ctypes.c_int
         L.pgw_sky_loop_noalloc_max_scratch.restype = sz
+        L.pgw_sky_probability.argtypes = [i32, i64, P, i64, P, P, P, P]
+        L.pgw_sky_probability.restype = ctypes.c_int
         for name in ("pgw_fp32_fma_peak", "pgw_calculate_dpf", "pgw_scan_sky_for_best_fit", "pgw_sky_loop",
                      "pgw_sky_loop_batched", "pgw_batch_get_td_vecs"):
             getattr(L, name).restype = ctypes.c_int
