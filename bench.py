@@ -162,6 +162,35 @@ def sky_tables_np(order: int):
     return ml, FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
 
 
+def workload_config(args, sizes, n_sky):
+    """The workload both arms run, the same dict in both JSON lines."""
+    return {"workload": (f"batched sky loop (regulator + scan), {args.clusters} clusters, "
+                         f"pixels log-uniform[20,3000], SNR U[8,40], HEALPix {args.order} "
+                         f"({n_sky} directions), L1/H1/V1, 41 delays, float32"),
+            "clusters": int(args.clusters), "total_pix": int(np.sum(sizes)), "n_sky": int(n_sky),
+            "healpix_order": int(args.order), "n_ifo": 3, "n_delay": 2 * K_TD + 1,
+            "seed": int(args.seed),
+            "l2": "inputs larger than L2: 2.4 GB td amplitudes + 35 GB maps per step"}
+
+
+N_CPU_SAMPLE = 32
+
+
+def sampled_clusters(seed, sizes, ml, FP_t, FX_t):
+    """The clusters both arms time on the CPU: a size-stratified sample of the
+    workload, each generated on the host from its own seed (seed, c), so the
+    reference arm and the GPU arm's batch hold identical data for them."""
+    from pycwb_gb300.autotune import sample_indices
+    from pycwb_gb300.synthetic import make_cluster
+    out = {}
+    for c in sample_indices(sizes, N_CPU_SAMPLE):
+        rng = np.random.default_rng([int(seed), int(c)])
+        td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, int(sizes[c]), K_TD,
+                                          float(rng.uniform(8, 40)))
+        out[int(c)] = (td00, td90, rms)
+    return out
+
+
 # --------------------------------------------------------------------------
 # CPU baseline (the oracle: the reference's loops restated in C, OpenMP)
 # --------------------------------------------------------------------------
@@ -295,6 +324,8 @@ def main():
                     help="skip the oracle comparison on three clusters of the timed batch")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-skystat", action="store_true",
+                    help="skip the statistics-at-the-maximum field")
     ap.add_argument("--no-td", action="store_true")
     ap.add_argument("--no-subnet", action="store_true",
                     help="skip the sub-network-cut sky loop field")
@@ -332,38 +363,39 @@ def main():
         rng = np.random.default_rng(args.seed)
         sizes = log_uniform_sizes(rng, args.clusters, 20, 3000)
         from pycwb_gb300.likelihoodWP.batched import ClusterBatch
-        from pycwb_gb300.synthetic import make_cluster
-        # the reference arm needs host data of only the sampled clusters
-        from pycwb_gb300.autotune import sample_indices
-        keep = set(int(c) for c in sample_indices(sizes, 32))
+        # the reference arm needs host data of only the sampled clusters, the
+        # same clusters the GPU arm's batch holds at those positions
+        views = sampled_clusters(args.seed, sizes, ml, FP_t, FX_t)
         batch = ClusterBatch.__new__(ClusterBatch)
         batch.sizes = sizes
-        views = {}
-        for c in sorted(keep):
-            td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, int(sizes[c]), K_TD,
-                                              float(rng.uniform(8, 40)))
-            views[c] = (td00, td90, rms)
         batch.cluster_views = lambda c: views[int(c)]
         cores = os.cpu_count() or 1
-        vals = []
+        vals, secs = [], []
         for step in range(args.warmup + args.steps):
-            dt, pairs, evals, idx = cpu_sample(batch, ml, FP_t, FX_t, reg, n_clusters=32,
-                                               n_dirs=256, seed=step)
+            dt, pairs, evals, idx = cpu_sample(batch, ml, FP_t, FX_t, reg,
+                                               n_clusters=N_CPU_SAMPLE, n_dirs=256, seed=step)
             if step >= args.warmup:
                 vals.append(pairs / dt / float(sizes.mean()))
+                secs.append(dt)
         v = float(np.median(vals))
+        n_sky = ml.shape[1]
         line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-                "config": {"workload": "batched sky loop, 4096 clusters P~logU[20,3000], "
-                                       f"HEALPix {args.order}, 3 ifo, 41 delays", "clusters": args.clusters},
+                "ms_per_step": float(np.median(secs)) * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": workload_config(args, sizes, n_sky),
+                "step": (f"one step = the oracle's regulator + scan of {N_CPU_SAMPLE} "
+                         "size-stratified clusters of the workload (identical to the GPU arm's "
+                         "clusters at those positions) on 256 random directions each; value = "
+                         "direction-pixel pairs per second / the workload's mean cluster size"),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                  "sample": "oracle float32 (a restatement of the reference's "
                                            "dpf.py/sky_stat.py/sky_scan.py loops; the reference's "
-                                           "own numba code cannot be installed offline) on 32 "
-                                           "size-stratified clusters x 256 random directions per "
-                                           "step, normalised by the workload's mean cluster size"},
+                                           "own numba code cannot be installed offline), OpenMP "
+                                           f"on {cores} threads, {N_CPU_SAMPLE} size-stratified "
+                                           "clusters x 256 random directions per step, "
+                                           "normalised by the workload's mean cluster size"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -410,6 +442,9 @@ def main():
     batch.rms.copy_(rms)
     del td00, td90, rms
     torch.cuda.synchronize()
+    # the clusters the CPU baselines time: identical data in both arms
+    for c, v in sampled_clusters(args.seed + 1000 * rank, sizes, ml, FP_t, FX_t).items():
+        batch.set_cluster(c, *v)
     t_gen = time.perf_counter() - t_gen
 
     shape = None if args.no_tune else autotune(tables, batch, fast_math=bool(args.fast_math))
@@ -540,6 +575,8 @@ def main():
     if rank == 0 and not args.no_parity:
         parity = parity_sample(res, batch, ml, FP_t, FX_t, reg, args.order)
 
+    skystat = (time_skystat(loop, res, batch, dev, args.seed + 3)
+               if not args.no_skystat else None)
     adjoint = time_adjoint(loop, res, batch, args.order, dev) if not args.no_adjoint else None
     td_build = time_td_build(dev) if not args.no_td else None
     wdm_field = time_wdm(dev) if not args.no_wdm else None
@@ -561,17 +598,10 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {
-                "workload": (f"batched sky loop (regulator + scan), {args.clusters} clusters, "
-                             f"pixels log-uniform[20,3000], SNR U[8,40], HEALPix {args.order} "
-                             f"({n_sky} directions), L1/H1/V1, 41 delays, float32"),
-                "clusters": args.clusters, "total_pix": total_pix, "n_sky": n_sky,
-                "healpix_order": args.order, "n_ifo": 3, "n_delay": 2 * K_TD + 1,
-                "launch_shape": dict(zip(("threads", "lanes_per_sky", "chunk_pix", "stages",
-                                          "min_blocks", "fast_math"), shape.key())),
-                "l2": "inputs larger than L2: 2.4 GB td amplitudes + 35 GB maps per step",
-                "generation_s": round(t_gen, 2),
-            },
+            "config": workload_config(args, sizes, n_sky),
+            "launch_shape": dict(zip(("threads", "lanes_per_sky", "chunk_pix", "stages",
+                                      "min_blocks", "fast_math"), shape.key())),
+            "generation_s": round(t_gen, 2),
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "ops_per_launch": useful_ops,
@@ -592,6 +622,7 @@ def main():
             "regulator_only_ms": reg_only_ms,
             "fast_math_variant": fast,
             "adjoint": adjoint,
+            "skystat": skystat,
             "td_build": td_build,
             "wdm": wdm_field,
             "pipeline": pipeline,
@@ -945,6 +976,76 @@ def time_subnet(dev, seed, n_clusters=1024, n_loud=200, order=4, reps=3):
             "cpu_oracle_evals_per_s": n_cpu * n_sky / cpu_s, "cpu_cores": 1,
             "cpu_sample": f"{n_cpu} clusters, float32 oracle, one thread",
             "selected": int((res["key"].reshape(-1) != 0).sum())}
+
+
+def synthetic_xtalk_rows(rng, sizes, n_nbr=4, scale=0.05):
+    """Packed xtalk overlaps for a batch (the overlap catalog is not
+    available): every pixel overlaps itself with (1, 0, 0, 1) and n_nbr
+    random pixels of its cluster with N(0, scale) coefficients; rows (n, 8)
+    float32 with cluster-local neighbour indices, lookup (total_pix, 2)."""
+    sizes = np.asarray(sizes, np.int64)
+    total = int(sizes.sum())
+    per = n_nbr + 1
+    owner_size = np.repeat(sizes, sizes)
+    rows = np.zeros((total, per, 8), np.float32)
+    local = np.concatenate([np.arange(P) for P in sizes]) if total else np.zeros(0, np.int64)
+    rows[:, 0, 0] = local
+    rows[:, 0, 4] = 1.0
+    rows[:, 0, 7] = 1.0
+    nb = (rng.random((total, n_nbr)) * owner_size[:, None]).astype(np.int64)
+    rows[:, 1:, 0] = nb
+    rows[:, 1:, 4:8] = rng.normal(0.0, scale, (total, n_nbr, 4))
+    lookup = np.stack([np.arange(total) * per, np.arange(total) * per + per], axis=1)
+    return rows.reshape(-1, 8), lookup.astype(np.int64)
+
+
+def time_skystat(loop, res, batch, dev, seed, reps=3):
+    """Statistics at the sky maximum (pgw_skystat_batched,
+    sky_statistics.py:94-262) of every cluster of the timed batch, one launch,
+    device-resident inputs and synthetic xtalk overlaps, CUDA-event timed."""
+    import ctypes
+    import torch
+    from pycwb_gb300 import _lib
+    from pycwb_gb300.likelihoodWP.sky_statistics import SKYSTAT_DTYPE
+
+    L = _lib.load()
+    t, b = loop.t, batch
+    n = b.n_clusters
+    xt_h, lk_h = synthetic_xtalk_rows(np.random.default_rng(seed), b.sizes)
+    s = loop.stream
+    with torch.cuda.stream(s):
+        xt = torch.from_numpy(xt_h).to(dev)
+        lk = torch.from_numpy(lk_h).to(dev)
+        l = torch.from_numpy(np.ascontiguousarray(res.l_max, np.int64)).to(dev)
+        regs = loop.regs.to(torch.float32)
+        ws = torch.empty(int(L.pgw_skystat_workspace_bytes(b.n_ifo, b.total_pix)),
+                         dtype=torch.uint8, device=dev)
+        out = torch.empty((n, SKYSTAT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    P = lambda x: ctypes.c_void_p(x.data_ptr())
+
+    def launch():
+        rc = L.pgw_skystat_batched(b.n_ifo, n, P(loop.pix_off), P(loop.td_off), b.total_pix,
+                                   t.n_sky, P(t.FP), P(t.FX), P(loop.rms), P(loop.td00),
+                                   P(loop.td90), b.n_delay, P(t.ml), P(l), P(regs),
+                                   float(t.REG0), float(t.network_energy_threshold), P(xt),
+                                   int(xt.shape[0]), P(lk), 0, P(ws), ws.numel(), P(out),
+                                   ctypes.c_void_p(s.cuda_stream))
+        if rc:
+            raise RuntimeError(L.pgw_last_error().decode())
+    launch()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        launch()
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    rec = np.frombuffer(out.cpu().numpy().tobytes(), dtype=SKYSTAT_DTYPE)
+    return {"workload": f"{n} clusters of the timed batch at their sky maxima, "
+                        f"{b.total_pix} pixels, 5 synthetic xtalk rows per pixel",
+            "ms": ms, "us_per_cluster": ms * 1e3 / n, "clusters_per_s": n / (ms * 1e-3),
+            "status_ok": int((rec["status"] == 0).sum())}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):

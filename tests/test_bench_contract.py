@@ -24,3 +24,7 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+    # a finite step time, and the workload the GPU arm prints
+    assert isinstance(d["ms_per_step"], float) and d["ms_per_step"] > 0
+    assert d["config"]["clusters"] == 64 and d["config"]["healpix_order"] == 7
+    assert d["config"]["n_sky"] == 196608 and d["config"]["total_pix"] > 0

@@ -178,3 +178,42 @@ def test_copy_from_host_is_exact(env, nbytes, offset):
     got = dst.cpu()
     assert torch.equal(got[offset:], src[offset:])
     assert int(got[:offset].sum()) == 0
+
+
+def test_many_small_clusters_order_in_workspace(oracle_mod):
+    """More clusters than the queue-order sort holds in shared memory (4,096):
+    the sort keys then live in the workspace.  Every cluster's REG[1] and
+    sky maximum must be the oracle's (checked on a spread of clusters)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pycwb_gb300 import _lib, sky
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch, SkyTables
+    from pycwb_gb300.synthetic import make_cluster, regulators
+    _lib.build()
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(["L1", "H1", "V1"], "L1", 512.0, 20,
+                                                    healpix_order=1)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    reg = regulators(3)
+    tables = SkyTables.from_arrays(FP_t, FX_t, ml, None, **{k: reg[k] for k in (
+        "network_energy_threshold", "gamma_regulator", "delta_regulator", "netCC")})
+    rng = np.random.default_rng(5000)
+    sizes = rng.integers(1, 6, 5000)
+    clusters = [make_cluster(rng, ml, FP_t, FX_t, int(P), 20, float(rng.uniform(8, 40)))[:3]
+                for P in sizes]
+    res = BatchedSkyLoop(tables, ClusterBatch.from_clusters(clusters)).run()
+    n_sky = ml.shape[1]
+    valid = np.arange(n_sky, dtype=np.int64)
+    REG0 = np.float32(reg["delta_regulator"] * math.sqrt(2))
+    for c in range(0, 5000, 97):
+        td00, td90, rms = clusters[c]
+        reg1 = oracle_mod.calculate_dpf(FP_t, FX_t, rms, n_sky, 3, reg["gamma_regulator"],
+                                        reg["network_energy_threshold"], valid)
+        assert np.float32(res.regulator[c]) == np.float32(reg1), c
+        REG = np.array([REG0, reg1, 0.0], np.float32)
+        ref = oracle_mod.scan_sky_for_best_fit(3, rms.shape[0], n_sky, FP_t, FX_t, rms, td00, td90,
+                                               ml, REG, reg["netCC"], reg["delta_regulator"],
+                                               reg["network_energy_threshold"], valid)
+        if ref[12] > 0 and int(res.l_max[c]) != ref[0]:     # only a near-tie may differ
+            a, b = float(ref[7][int(res.l_max[c])]), float(ref[7][ref[0]])
+            assert abs(a - b) <= 1e-5 * abs(b), (c, a, b)
