@@ -31,11 +31,13 @@ _lock = threading.Lock()
 
 
 def candidates(n_ifo: int, fast_math: bool):
+    """Launch shapes to try; fast_math selects the scan's arithmetic (True:
+    refined division and approximate square root, False: IEEE rounding)."""
     out = []
     minbs = (3, 4) if n_ifo <= 4 else (2,)
     for threads, lanes, stages, chunk, minb in itertools.product((128, 256), (1, 2), (2, 3),
                                                                   (0, 16), minbs):
-        out.append(_lib.TileShape(threads, lanes, chunk, stages, minb, int(fast_math)))
+        out.append(_lib.TileShape(threads, lanes, chunk, stages, minb, 1 if fast_math else -1))
     return out
 
 
@@ -99,7 +101,7 @@ def sample_indices(sizes, n_sample=48, seed=0):
     return np.sort(order[pick])
 
 
-def autotune(tables, batch, fast_math=False, n_sample=48, reps=2, use_cache=True, verbose=False):
+def autotune(tables, batch, fast_math=True, n_sample=48, reps=2, use_cache=True, verbose=False):
     """Best TileShape for this tables/batch problem class (measured)."""
     from .likelihoodWP.batched import BatchedSkyLoop, ClusterBatch
 

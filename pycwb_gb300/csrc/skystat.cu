@@ -84,6 +84,28 @@ template <int I> struct DW {
                        gdat = 6 * I, gnul = 7 * I, rnx = 8 * I, stride = 8 * I + 1;
 };
 
+// Sum over the CTA of N float64 values per thread; every thread gets the
+// totals.  The order differs from a pixel-order loop, so results agree with
+// it to float64 rounding.
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N], double (*red)[kThreads / 32]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[k][w] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double t = 0.0;
+    for (int u = 0; u < kThreads / 32; ++u) t += red[k][u];
+    v[k] = t;
+  }
+  __syncthreads();
+}
+
 template <int I>
 __device__ void xtalk_terms(const StatArgs& a, int64_t gp, int64_t P, const double* pv,
                             const double* qv, int pstride, double (&x0)[I], double (&x1)[I],
@@ -255,41 +277,45 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
   }
   __syncthreads();
 
-  // 2. packet rotations of data and signal (avx_packet_ps), pixel order
+  // 2. packet rotations of data and signal (avx_packet_ps).  The packet sums
+  // are float32 loops over the pixels in pixel order in the reference; each of
+  // the 2 x I (packet, detector) loops runs on its own thread, in that order.
   __shared__ float s_E[2][8];       // per-detector packet energies (data, signal)
+  if (threadIdx.x < 2 * I) {
+    const int which = threadIdx.x / I, i = threadIdx.x % I;
+    const int o0 = which == 0 ? W::v0 : W::s, o9 = which == 0 ? W::v9 : W::Sg;
+    float (*k)[8] = which == 0 ? s_pk : s_sk;
+    float aa = 0.f, AA = 0.f, aA = 0.f;
+    for (int64_t j = 0; j < P; ++j) {
+      const float* w = wf + j * W::stride;
+      const float m = w[W::msk] > 0.0f ? 1.0f : 0.0f;
+      const float x = w[o0 + i], y = w[o9 + i];
+      aa = A(aa, M(m, M(x, x)));
+      AA = A(AA, M(m, M(y, y)));
+      aA = A(aA, M(m, M(x, y)));
+    }
+    const float s2 = M(2.0f, aA), c2 = S(aa, AA);
+    const float x = A(A(aa, AA), 1e-9f);
+    // the norm is a float64 (Python) value; float32 operands round it first
+    const double nn = __dsqrt_rn(static_cast<double>(A(M(c2, c2), M(s2, s2))));
+    const float nnf = static_cast<float>(nn);
+    const float av = static_cast<float>(__dsqrt_rn(static_cast<double>(D(A(x, nnf), 2.0f))));
+    const float Av = static_cast<float>(
+        __dsqrt_rn(static_cast<double>(fabsf(D(S(x, nnf), 2.0f)))));
+    const float cc = D(c2, static_cast<float>(dA(nn, 1e-9)));
+    const float sgn = s2 > 0.0f ? 1.0f : -1.0f;
+    k[0][i] = static_cast<float>(__dsqrt_rn(static_cast<double>(D(S(1.0f, cc), 2.0f))));
+    k[1][i] = M(static_cast<float>(__dsqrt_rn(static_cast<double>(D(A(1.0f, cc), 2.0f)))), sgn);
+    k[2][i] = D(1.0f, A(av, 1e-9f));
+    k[3][i] = D(1.0f, A(Av, 1e-9f));
+    const float sum = A(av, Av);
+    s_aA[which][i] = sum;
+    s_E[which][i] = D(M(sum, sum), 2.0f);
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     for (int which = 0; which < 2; ++which) {
-      const int o0 = which == 0 ? W::v0 : W::s, o9 = which == 0 ? W::v9 : W::Sg;
-      float (*k)[8] = which == 0 ? s_pk : s_sk;
       float Ep = 0.f;
-      for (int i = 0; i < I; ++i) {
-        float aa = 0.f, AA = 0.f, aA = 0.f;
-        for (int64_t j = 0; j < P; ++j) {
-          const float* w = wf + j * W::stride;
-          const float m = w[W::msk] > 0.0f ? 1.0f : 0.0f;
-          const float x = w[o0 + i], y = w[o9 + i];
-          aa = A(aa, M(m, M(x, x)));
-          AA = A(AA, M(m, M(y, y)));
-          aA = A(aA, M(m, M(x, y)));
-        }
-        const float s2 = M(2.0f, aA), c2 = S(aa, AA);
-        const float x = A(A(aa, AA), 1e-9f);
-        // the norm is a float64 (Python) value; float32 operands round it first
-        const double nn = __dsqrt_rn(static_cast<double>(A(M(c2, c2), M(s2, s2))));
-        const float nnf = static_cast<float>(nn);
-        const float av = static_cast<float>(__dsqrt_rn(static_cast<double>(D(A(x, nnf), 2.0f))));
-        const float Av = static_cast<float>(
-            __dsqrt_rn(static_cast<double>(fabsf(D(S(x, nnf), 2.0f)))));
-        const float cc = D(c2, static_cast<float>(dA(nn, 1e-9)));
-        const float sgn = s2 > 0.0f ? 1.0f : -1.0f;
-        k[0][i] = static_cast<float>(__dsqrt_rn(static_cast<double>(D(S(1.0f, cc), 2.0f))));
-        k[1][i] = M(static_cast<float>(__dsqrt_rn(static_cast<double>(D(A(1.0f, cc), 2.0f)))), sgn);
-        k[2][i] = D(1.0f, A(av, 1e-9f));
-        k[3][i] = D(1.0f, A(Av, 1e-9f));
-        const float sum = A(av, Av);
-        s_aA[which][i] = sum;
-        s_E[which][i] = D(M(sum, sum), 2.0f);
-      }
       for (int i = 0; i < I; ++i) Ep = A(Ep, s_E[which][i]);
       if (which == 0) a.out[c].Eo = D(Ep, 2.0f);
       else a.out[c].Lo = D(Ep, 2.0f);
@@ -343,22 +369,20 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
   }
   __syncthreads();
 
-  // 4. detector norms, signal SNR, noise correction (thread 0, pixel order)
+  // 4. detector norms, signal SNR, noise correction: per-pixel terms on every
+  // thread, float64 sums as block reductions
+  __shared__ double s_red[16][kThreads / 32];
   __shared__ double s_norm[8];
   __shared__ double s_sc[8];   // GN, EC, SC, RC, NC, NS, EH, ES
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < I; ++i) {
-      double n = 0.0;
-      for (int64_t j = 0; j < P; ++j) n = dA(n, wd[j * Q::stride + Q::tcl + i]);
-      s_norm[i] = n < 2.0 ? 2.0 : n;
-    }
-    for (int i = 0; i < PGW_MAX_IFO; ++i)   // gw_norm_numpy: 2 E_signal / data norm
-      a.out[c].S_snr[i] = i < I ? static_cast<float>(
-          dD(static_cast<double>(M(s_E[1][i], 2.0f)), s_norm[i])) : 0.0f;
-    double GN = 0, EC = 0, SC = 0, RC = 0, NC = 0, NS = 0, EH = 0, ES = 0;
-    for (int64_t j = 0; j < P; ++j) {
+  {
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.0;
+    for (int64_t j = threadIdx.x; j < P; j += blockDim.x) {
       float* w = wf + j * W::stride;
       const double* d = wd + j * Q::stride;
+#pragma unroll
+      for (int i = 0; i < I; ++i) v[8 + i] = dA(v[8 + i], d[Q::tcl + i]);
       const float ec = w[W::ec];
       double ns = 0.0, nx = 0.0;
       for (int i = 0; i < I; ++i) {
@@ -369,9 +393,9 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
       nx = dD(nx, static_cast<double>(I));
       const double mk = w[W::msk] > 0.0f ? 1.0 : 0.0;
       const double core = dM(mk, nx > 0.0 ? 1.0 : 0.0);
-      EC = dA(EC, dM(core, ec));
-      NC = dA(NC, core);
-      ES = dA(ES, dM(dS(mk, core), d[Q::rnx]));
+      v[1] = dA(v[1], dM(core, ec));                     // EC
+      v[4] = dA(v[4], core);                             // NC
+      v[7] = dA(v[7], dM(dS(mk, core), d[Q::rnx]));      // ES
       const double gn = w[W::gn];
       double rc = gn < 2.0 ? 1.0 : 0.0;
       rc = dA(rc, dM(dM(gn, dS(1.0, rc)), 0.5));
@@ -379,14 +403,20 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
       const double sig = dM(mk, ns > 0.0 ? 1.0 : 0.0);
       const float gnew = static_cast<float>(dM(dM(mk, gn), nx));
       w[W::gn] = gnew;
-      SC = dA(SC, dM(sig, ec));
-      RC = dA(RC, dM(sig, rc));
-      GN = dA(GN, dM(sig, static_cast<double>(gnew)));
-      NS = dA(NS, sig);
-      EH = dA(EH, dM(dS(mk, sig), static_cast<double>(w[W::et])));
+      v[2] = dA(v[2], dM(sig, ec));                      // SC
+      v[3] = dA(v[3], dM(sig, rc));                      // RC
+      v[0] = dA(v[0], dM(sig, static_cast<double>(gnew)));  // GN
+      v[5] = dA(v[5], sig);                              // NS
+      v[6] = dA(v[6], dM(dS(mk, sig), static_cast<double>(w[W::et])));  // EH
     }
-    s_sc[0] = GN; s_sc[1] = EC; s_sc[2] = SC; s_sc[3] = RC; s_sc[4] = NC; s_sc[5] = NS;
-    s_sc[6] = EH; s_sc[7] = ES;
+    block_sum<16>(v, s_red);
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < I; ++i) s_norm[i] = v[8 + i] < 2.0 ? 2.0 : v[8 + i];
+      for (int i = 0; i < PGW_MAX_IFO; ++i)   // gw_norm_numpy: 2 E_signal / data norm
+        a.out[c].S_snr[i] = i < I ? static_cast<float>(
+            dD(static_cast<double>(M(s_E[1][i], 2.0f)), s_norm[i])) : 0.0f;
+      for (int k = 0; k < 8; ++k) s_sc[k] = v[k];
+    }
   }
   __syncthreads();
 
@@ -458,24 +488,41 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
   }
   __syncthreads();
 
-  // 6. event statistics (sky_statistics.py:196-262)
-  if (threadIdx.x == 0) {
-    double Em = 0.0, Np = 0.0, Npix = 0.0;
+  // 6. event statistics (sky_statistics.py:196-262): the per-detector sums of
+  // the xtalk energies and the effective pixel count as block reductions
+  double v6[17];
+#pragma unroll
+  for (int k = 0; k < 17; ++k) v6[k] = 0.0;
+  for (int64_t j = threadIdx.x; j < P; j += blockDim.x) {
+    const float* w = wf + j * W::stride;
+    const double* d = wd + j * Q::stride;
+    double q = 0.0;
+#pragma unroll
     for (int i = 0; i < I; ++i) {
-      double gd = 0.0, gz = 0.0;
-      for (int64_t j = 0; j < P; ++j) {
-        gd = dA(gd, wd[j * Q::stride + Q::gdat + i]);
-        gz = dA(gz, wd[j * Q::stride + Q::gnul + i]);
-      }
-      Em = dA(Em, gd);
-      Np = dA(Np, gz);
+      v6[i] = dA(v6[i], d[Q::gdat + i]);
+      v6[8 + i] = dA(v6[8 + i], d[Q::gnul + i]);
+      q = dA(q, d[Q::qn + i]);
     }
-    for (int64_t j = 0; j < P; ++j) {
-      const float* w = wf + j * W::stride;
-      double q = 0.0;
-      for (int i = 0; i < I; ++i) q = dA(q, wd[j * Q::stride + Q::qn + i]);
-      Npix = dA(Npix, dM(q, w[W::msk] > 0.0f ? 0.5 : 0.0));
+    v6[16] = dA(v6[16], dM(q, w[W::msk] > 0.0f ? 0.5 : 0.0));
+  }
+  {
+    double lo[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) lo[k] = v6[k];
+    block_sum<16>(lo, s_red);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v6[k] = lo[k];
+    double one[1] = {v6[16]};
+    block_sum<1>(one, s_red);
+    v6[16] = one[0];
+  }
+  if (threadIdx.x == 0) {
+    double Em = 0.0, Np = 0.0;
+    for (int i = 0; i < I; ++i) {
+      Em = dA(Em, v6[i]);
+      Np = dA(Np, v6[8 + i]);
     }
+    const double Npix = v6[16];
     const double Neff = dS(dD(dM(Npix, 4.0), static_cast<double>(I)), 1.0);
     const double GN = s_sc[0], EC = s_sc[1], SC = s_sc[2], RC = s_sc[3];
     const double EH = dD(s_sc[6], 2.0), ES = dD(s_sc[7], 2.0);

@@ -45,7 +45,7 @@ def _clusters(env, sizes, seed):
     return out
 
 
-@pytest.mark.parametrize("spec", [None, (256, 2, 0, 3, 4, 0), (128, 1, 7, 2, 4, 1)])
+@pytest.mark.parametrize("spec", [None, (256, 2, 0, 3, 4, -1), (128, 1, 7, 2, 4, 1)])
 def test_batched_matches_oracle_and_plain(env, oracle_mod, spec):
     from pycwb_gb300._lib import TileShape
     from pycwb_gb300.likelihoodWP import sky_loop
