@@ -618,7 +618,7 @@ def main():
                                         "2 flops per FMA) in this run"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 4 * args.steps,  # init, pack, suffix sums, sky loop
+            "gpu_launches": 2 * args.steps,  # set-up (prepare_kernel), sky loop
             "clocks": clk,
             "plain": plain,
             "batched_vs_plain": (plain["ms"] / ms_per_step) if plain else None,
@@ -1094,7 +1094,7 @@ def time_plain(L, loop, tables, batch, shape, dev):
     e1.record(s)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    return {"ms": ms, "launches": batch.n_clusters * 4,  # init, pack, suffix sums, sky loop
+    return {"ms": ms, "launches": batch.n_clusters * 2,  # set-up, sky loop
             "note": "same kernel, one pgw_sky_loop per cluster with the default one-cluster "
                     "launch shape, device-resident, 1 timed pass"}
 

@@ -126,10 +126,10 @@ int pgw_scan_sky_for_best_fit(int n_ifo, int64_t n_pix, int64_t n_sky, const flo
  *   stages         chunks in flight per CTA, 2..4
  *   min_blocks     occupancy target the kernel is compiled for: 3 or 4 CTAs
  *                  per SM for n_ifo <= 4, 2 above
- *   fast_math      0 (automatic) or 1: the scan divides by a reciprocal
- *                  estimate with one correction step (Markstein; within one
- *                  ulp of the correctly rounded quotient) and takes square
- *                  roots with sqrt.approx.f32; -1: IEEE rounding of every
+ *   fast_math      0 (automatic) or 1: the scan's divisions and square
+ *                  roots are a hardware estimate with one correction step
+ *                  (Markstein; within one ulp of the correctly rounded
+ *                  result, no slow-path branch); -1: IEEE rounding of every
  *                  division and square root.  Both meet the 1e-4 relative
  *                  parity bar; the regulator's decisions are exact either way
  *                  (its fallback always uses IEEE arithmetic). */
