@@ -175,6 +175,11 @@ def workload_config(args, sizes, n_sky):
 
 N_CPU_SAMPLE = 32
 
+# Per-warp pixel iterations the regulator runs, as a fraction of the full
+# sum over (direction, pixel) pairs, counted in a diagnostic build on 1,024
+# clusters of this workload (its early decisions stop the rest).
+REG_ITER_FRACTION = 0.458
+
 
 def sampled_clusters(seed, sizes, ml, FP_t, FX_t):
     """The clusters both arms time on the CPU: a size-stratified sample of the
@@ -613,6 +618,14 @@ def main():
                                       f"({active / work_pairs:.3%} of pairs)"),
                          "reference_ops_per_launch": ops,
                          "reference_equivalent_tflops": ops / (kernel_ms * 1e-3) / 1e12,
+                         "frac_regulator_as_executed": (
+                             (REG_ITER_FRACTION * reg_ops(3) * work_pairs + scan_ops(3) * active)
+                             / (kernel_ms * 1e-3) / 1e12 / peak) if peak else None,
+                         "frac_regulator_as_executed_note": (
+                             f"the regulator credited only for the {REG_ITER_FRACTION:.1%} of its "
+                             "per-warp pixel iterations that run (its early pass/fail "
+                             "decisions stop the rest; fraction counted on 1,024 clusters of this "
+                             "workload in a diagnostic build)"),
                          "kernel_ms": kernel_ms,
                          "peak_source": "measured: pgw_fp32_fma_peak (register FMA chains, "
                                         "2 flops per FMA) in this run"},
@@ -1045,10 +1058,32 @@ def time_skystat(loop, res, batch, dev, seed, reps=3):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
     rec = np.frombuffer(out.cpu().numpy().tobytes(), dtype=SKYSTAT_DTYPE)
+    # the sky probability (softmax of nSkyStat) of 256 clusters' maps
+    n_p = min(256, n)
+    with torch.cuda.stream(s):
+        sel = torch.arange(n_p, dtype=torch.int32, device=dev)
+        prob = torch.empty((n_p, t.n_sky), dtype=torch.float32, device=dev)
+        summ = torch.empty((n_p, 4), dtype=torch.float64, device=dev)
+
+    def prob_launch():
+        rc = L.pgw_sky_probability(n_p, t.n_sky, loop.stats.data_ptr(), int(loop.stats.stride(0)),
+                                   sel.data_ptr(), prob.data_ptr(), summ.data_ptr(),
+                                   ctypes.c_void_p(s.cuda_stream))
+        if rc:
+            raise RuntimeError(L.pgw_last_error().decode())
+    prob_launch()
+    e0.record(s)
+    prob_launch()
+    e1.record(s)
+    e1.synchronize()
+    prob_ms = e0.elapsed_time(e1)
     return {"workload": f"{n} clusters of the timed batch at their sky maxima, "
                         f"{b.total_pix} pixels, 5 synthetic xtalk rows per pixel",
             "ms": ms, "us_per_cluster": ms * 1e3 / n, "clusters_per_s": n / (ms * 1e-3),
-            "status_ok": int((rec["status"] == 0).sum())}
+            "status_ok": int((rec["status"] == 0).sum()),
+            "probability_ms": prob_ms, "probability_maps": n_p,
+            "probability_note": "pgw_sky_probability: float64 softmax of nSkyStat and the 50 % / "
+                                "90 % direction counts, one launch over n maps"}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):

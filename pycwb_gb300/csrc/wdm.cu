@@ -19,7 +19,9 @@
 // One CTA transforms G = max(1, 2048 / 2M) consecutive slices: the fold
 // reads the series coalesced along m and writes the folded values in
 // bit-reversed order to shared memory; a radix-2 decimation-in-time FFT of
-// length 2M runs there in float64 with twiddles from sincospi; the M+1
+// length 2M runs there in float64 with twiddles from one table per device
+// (W_8192^j, j < 4096, from sincospi; the twiddle W_2M^k of any M <= 4096 is
+// entry k 4096/M, the same angle to the last bit); the M+1
 // outputs of each slice are written as float64 maps (n, m) and/or as the
 // zero-padded float32 planes that the td-amplitude build reads.  All work is
 // float64; the fold costs 2 nW / M FMAs per input sample and the FFT
@@ -29,6 +31,7 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 
 #include "../../include/pycwb_gb300.h"
@@ -42,6 +45,19 @@ namespace {
 constexpr double kSqrt2 = 1.4142135623730951;  // the double nearest sqrt(2)
 constexpr int kSlicePoints = 2048;              // complex points per CTA (G * 2M)
 constexpr int kThreads = 256;
+constexpr int kMaxM = 4096;
+
+// W_8192^j = exp(-2 pi i j / 8192), j < 4096, on every device that loads the
+// library (64 KB), filled once per device by twiddle_init_kernel.
+__device__ double2 g_wdm_twiddle[kMaxM];
+
+__global__ void twiddle_init_kernel() {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= kMaxM) return;
+  double s, c;
+  sincospi(static_cast<double>(j) / static_cast<double>(kMaxM), &s, &c);
+  g_wdm_twiddle[j] = make_double2(c, -s);
+}
 
 __device__ __forceinline__ double series_at(const double* __restrict__ x, int64_t n_ts, int64_t s) {
   if (s < 0) s = -s;                    // x(-k) = x(k)
@@ -62,11 +78,8 @@ wdm_t2w_kernel(const double* __restrict__ x, int64_t n_ts, int M, int log2M2,
   const int64_t n0 = static_cast<int64_t>(blockIdx.x) * G;
   const int64_t kfold = (n_filter - 1) / M2;  // filter spans t in [-kfold*M2, kfold*M2]
 
-  for (int k = threadIdx.x; k < half; k += blockDim.x) {
-    double s, c;
-    sincospi(static_cast<double>(k) / static_cast<double>(M), &s, &c);  // angle 2 pi k / 2M
-    tw[k] = make_double2(c, -s);
-  }
+  const int tw_step = kMaxM / M;               // W_2M^k = W_8192^(k 4096 / M)
+  for (int k = threadIdx.x; k < half; k += blockDim.x) tw[k] = g_wdm_twiddle[k * tw_step];
 
   // fold, stored bit-reversed for the in-place decimation-in-time FFT
   const int shift = 32 - log2M2;
@@ -169,6 +182,33 @@ extern "C" int pgw_wdm_t2w(const double* ts, int64_t n_ts, int M, const double* 
   if (blocks > 0x7fffffffLL) return pgw::fail(PGW_ERR_BAD_SHAPE, "series too long");
   const size_t smem = sizeof(double2) * (static_cast<size_t>(M) + static_cast<size_t>(G) * M2);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The twiddle table, once per device: filled on the caller's stream and
+  // waited for, so later calls on any stream find it complete.  A first call
+  // made while the stream is being captured puts the fill in the graph and
+  // leaves the table marked empty, so the next ordinary call fills it again.
+  {
+    static std::mutex mu;
+    static bool ready[256] = {false};
+    int dev = 0;
+    cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess || dev < 0 || dev >= 256)
+      return pgw::fail(PGW_ERR_CUDA, "cudaGetDevice failed for the WDM twiddle table");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ready[dev]) {
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      de = cudaStreamIsCapturing(s, &cap);
+      if (de != cudaSuccess)
+        return pgw::fail(PGW_ERR_CUDA, std::string("wdm twiddles: ") + cudaGetErrorString(de));
+      twiddle_init_kernel<<<kMaxM / kThreads, kThreads, 0, s>>>();
+      de = cudaGetLastError();
+      if (de == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        de = cudaStreamSynchronize(s);
+        if (de == cudaSuccess) ready[dev] = true;
+      }
+      if (de != cudaSuccess)
+        return pgw::fail(PGW_ERR_CUDA, std::string("wdm twiddles: ") + cudaGetErrorString(de));
+    }
+  }
   cudaError_t e = cudaFuncSetAttribute(wdm_t2w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess)
