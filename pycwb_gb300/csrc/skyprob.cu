@@ -32,7 +32,6 @@ namespace {
 
 constexpr int kThreads = 1024;
 constexpr int kStatRow = 6;        // nSkyStat in the (11, n_sky) block
-constexpr int kBisect = 40;        // threshold bisection steps (relative width 1e-12)
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -92,27 +91,30 @@ __global__ void __launch_bounds__(kThreads) sky_probability_kernel(
 
   // Error-region inputs: the smallest set of directions, largest
   // probabilities first, holding at least 50 % / 90 % of the total.  The
-  // probability threshold t is bisected (in the float32 values just written)
-  // until the mass above it brackets each level; the count is taken at the
-  // upper end of the final bracket.
+  // probabilities are non-negative floats, whose bit patterns order as
+  // unsigned integers, so the threshold is bisected over the bit patterns:
+  // the largest pattern lo with mass(p >= lo) >= level, exact after about
+  // 30 steps.  Each step sums the mass above the trial pattern in float32
+  // per thread (the FP64 pipe is narrow on this GPU) and in float64 across
+  // the block.
   __syncthreads();
   const double levels[2] = {0.5, 0.9};
   double counts[2] = {0.0, 0.0};
   if (!nan) {
     for (int q = 0; q < 2; ++q) {
-      double lo = 0.0, hi = 1.0;   // mass(>= hi) < level <= mass(>= lo)
-      for (int it = 0; it < kBisect; ++it) {
-        const double t = 0.5 * (lo + hi);
-        double m = 0.0;
+      unsigned lo = 0u, hi = 0x7f800000u;   // mass(>= hi) = 0 < level <= mass(>= lo)
+      while (hi - lo > 1u) {
+        const unsigned mid = lo + ((hi - lo) >> 1);
+        float m = 0.0f;
         for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x) {
-          const double p = static_cast<double>(out[l]);
-          if (p >= t) m += p;
+          const float p = out[l];
+          if (__float_as_uint(p) >= mid) m += p;
         }
-        m = block_sum(m, red);
-        if (m >= levels[q]) lo = t; else hi = t;
+        const double tot = block_sum(static_cast<double>(m), red);
+        if (tot >= levels[q]) lo = mid; else hi = mid;
       }
       double n = 0.0;
-      for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x) n += static_cast<double>(out[l]) >= lo;
+      for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x) n += __float_as_uint(out[l]) >= lo;
       counts[q] = block_sum(n, red);
     }
   }
