@@ -8,9 +8,11 @@
 // over all n_sky entries (masked directions hold 0 and take part).  Here
 // one CTA per selected cluster reads that cluster's map where the sky loop
 // left it (stats block (11, n_sky), row 6) and writes the float32
-// probabilities; the maximum and the sum are float64 as in the reference
-// (the sum is a block reduction, so it agrees with NumPy's pairwise sum to
-// float64 rounding).  NaN anywhere in the map makes every probability NaN,
+// probabilities; the maximum, the sum and the normalisation are float64 as
+// in the reference (the sum is a block reduction, so it agrees with NumPy's
+// pairwise sum to float64 rounding), the exponentials float32-accurate
+// (exp_neg), so a probability agrees with the reference's to a few float32
+// ulp.  NaN anywhere in the map makes every probability NaN,
 // as NumPy's max and sum propagate it.  Alongside, per cluster: the maximum,
 // the sum and the number of directions whose probabilities, taken largest
 // first, reach 50 % and 90 % of the total -- the inputs of an error region
@@ -65,6 +67,19 @@ __device__ __forceinline__ double block_max(double v, double* red) {
 
 __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
 
+// exp(d) for d <= 0 to float32 accuracy without a float64 exponential (the
+// float64 pipe is narrow on this GPU): Cody-Waite range reduction in float64,
+// d = k ln2 + r with k = rint(d / ln2) and |r| <= ln2 / 2 (r exact to about
+// 1e-16 |d| by one FMA with the double nearest ln2), then exp(r) in float32
+// and the exact scaling by 2^k.  Within about 2 ulp of float(exp(d)); 0 below
+// the smallest float32 (d < -104).
+__device__ __forceinline__ float exp_neg(double d) {
+  if (!(d > -104.0)) return 0.0f;
+  const double k = rint(d * 1.4426950408889634);       // 1 / ln 2
+  const float r = static_cast<float>(fma(-k, 0.6931471805599453, d));
+  return ldexpf(expf(r), static_cast<int>(k));
+}
+
 __global__ void __launch_bounds__(kThreads) sky_probability_kernel(
     int64_t n_sky, const float* __restrict__ stats, int64_t stats_stride,
     const int32_t* __restrict__ clusters, float* __restrict__ prob, double* __restrict__ summary) {
@@ -82,12 +97,16 @@ __global__ void __launch_bounds__(kThreads) sky_probability_kernel(
   }
   nan = block_or(nan);
   mx = block_max(mx, red);
+  // the exponentials are float32-accurate (exp_neg); the sum and the
+  // normalisation stay float64, as the reference's
   double sum = 0.0;
   if (!nan)
-    for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x) sum += exp(static_cast<double>(s[l]) - mx);
+    for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x)
+      sum += static_cast<double>(exp_neg(static_cast<double>(s[l]) - mx));
   sum = nan ? NAN : block_sum(sum, red);
   for (int64_t l = threadIdx.x; l < n_sky; l += blockDim.x)
-    out[l] = nan ? NAN : static_cast<float>(exp(static_cast<double>(s[l]) - mx) / sum);
+    out[l] = nan ? NAN
+                 : static_cast<float>(static_cast<double>(exp_neg(static_cast<double>(s[l]) - mx)) / sum);
 
   // Error-region inputs: the smallest set of directions, largest
   // probabilities first, holding at least 50 % / 90 % of the total.  The
