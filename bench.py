@@ -1016,9 +1016,11 @@ def synthetic_xtalk_rows(rng, sizes, n_nbr=4, scale=0.05):
 
 
 def time_skystat(loop, res, batch, dev, seed, reps=3):
-    """Statistics at the sky maximum (pgw_skystat_batched,
-    sky_statistics.py:94-262) of every cluster of the timed batch, one launch,
-    device-resident inputs and synthetic xtalk overlaps, CUDA-event timed."""
+    """The reference caller's per-cluster consumers of the sky maps, on the
+    device, CUDA-event timed: the statistics at the sky maximum
+    (pgw_skystat_batched, sky_statistics.py:94-262) of every cluster of the
+    timed batch in one launch (synthetic xtalk overlaps), and the sky
+    probability of every cluster with sky_stat_max > 0 in one launch."""
     import ctypes
     import torch
     from pycwb_gb300 import _lib
@@ -1058,10 +1060,13 @@ def time_skystat(loop, res, batch, dev, seed, reps=3):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
     rec = np.frombuffer(out.cpu().numpy().tobytes(), dtype=SKYSTAT_DTYPE)
-    # the sky probability (softmax of nSkyStat) of 256 clusters' maps
-    n_p = min(256, n)
+    # the sky probability (softmax of nSkyStat) of every cluster the
+    # reference's caller computes it for: those with sky_stat_max > 0
+    # (likelihood.py:328-342)
+    keep = np.flatnonzero(res.found & (res.sky_stat_max > 0)).astype(np.int32)
+    n_p = int(keep.size)
     with torch.cuda.stream(s):
-        sel = torch.arange(n_p, dtype=torch.int32, device=dev)
+        sel = torch.from_numpy(keep).to(dev)
         prob = torch.empty((n_p, t.n_sky), dtype=torch.float32, device=dev)
         summ = torch.empty((n_p, 4), dtype=torch.float64, device=dev)
 
@@ -1082,8 +1087,9 @@ def time_skystat(loop, res, batch, dev, seed, reps=3):
             "ms": ms, "us_per_cluster": ms * 1e3 / n, "clusters_per_s": n / (ms * 1e-3),
             "status_ok": int((rec["status"] == 0).sum()),
             "probability_ms": prob_ms, "probability_maps": n_p,
-            "probability_note": "pgw_sky_probability: float64 softmax of nSkyStat and the 50 % / "
-                                "90 % direction counts, one launch over n maps"}
+            "probability_note": "pgw_sky_probability: softmax of nSkyStat (float32-accurate "
+                                "exponentials, float64 sum) and the 50 % / 90 % direction counts "
+                                "of every cluster with sky_stat_max > 0, one launch"}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):
