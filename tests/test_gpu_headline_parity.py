@@ -164,3 +164,46 @@ def test_batched_order7_size_stratified(sky7, oracle_mod):
         got = res.cluster_tuple(c)
         _check_cluster(oracle_mod, e, got, res.regulator[c], td00, td90, rms, rng,
                        f"batched cluster {c} (P={rms.shape[0]})")
+
+
+def test_plain_order8_four_detectors_wide_window(oracle_mod):
+    """Config 5's sky and detectors: HEALPix 8 (786,432 directions),
+    L1/H1/V1/K1, K = 67 (135 delays), one 800-pixel cluster: REG[1] equal
+    over the whole sky, the maps on a sample plus the maximum's
+    neighbourhood, the maximum identical."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pycwb_gb300 import _lib, sky
+    from pycwb_gb300.likelihoodWP import sky_loop
+    from pycwb_gb300.synthetic import make_cluster, regulators
+    _lib.build()
+    ifos = ("L1", "H1", "V1", "K1")
+    K8 = 67
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(list(ifos), ifos[0], 2048.0, K8,
+                                                    healpix_order=8)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    phi, lat = sky.build_sky_directions(ml.shape[1], healpix_order=8)
+    xyz = np.stack([np.cos(lat) * np.cos(phi), np.cos(lat) * np.sin(phi), np.sin(lat)], axis=1)
+    e = dict(ml=ml, FP_t=FP_t, FX_t=FX_t, reg=regulators(len(ifos)), xyz=xyz, n_sky=ml.shape[1],
+             valid=np.arange(ml.shape[1], dtype=np.int64))
+    rng = np.random.default_rng(88)
+    td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, 800, K8, 20.0)
+    r = e["reg"]
+    REG0 = np.float32(r["delta_regulator"] * math.sqrt(2))
+    reg, out = sky_loop(len(ifos), 800, e["n_sky"], FP_t, FX_t, rms, td00, td90, ml, REG0,
+                        r["gamma_regulator"], r["netCC"], r["network_energy_threshold"],
+                        e["valid"])
+    reg1 = oracle_mod.calculate_dpf(FP_t, FX_t, rms, e["n_sky"], len(ifos), r["gamma_regulator"],
+                                    r["network_energy_threshold"], e["valid"])
+    assert np.float32(reg) == np.float32(reg1)
+    sub = _sample(e, rng, [out[0]])
+    REG = np.array([REG0, reg1, 0.0], np.float32)
+    args = (len(ifos), 800, e["n_sky"], FP_t, FX_t, rms, td00, td90, ml)
+    tail = (r["netCC"], r["delta_regulator"], r["network_energy_threshold"], sub)
+    ref = oracle_mod.scan_sky_for_best_fit(*args, REG, *tail, return_ellipticity=True)
+    f64 = oracle_mod.scan_sky_for_best_fit(*args, REG.astype(np.float64), *tail, precision="f64",
+                                           return_ellipticity=True)
+    cmp = _restrict(out, sub)
+    assert_scan_close(cmp, ref, f64, ref_cr=ref[13], netCC=r["netCC"], what="order 8, 4 ifo, K 67")
+    assert f64_error_ratio(cmp, ref, f64) <= 3.0
