@@ -390,6 +390,20 @@ int pgw_skystat_batched(int n_ifo, int n_clusters, const int64_t* pix_offsets,
                         int64_t n_xtalk, const int64_t* xtalk_lookup, int xgb_rho_mode, void* ws,
                         size_t ws_bytes, pgw_skystat_result* out, void* stream);
 
+/* The per-pixel arrays of the reference's SkyStatistics
+ * (sky_statistics.py:264-292) for every pixel of the clusters of the last
+ * pgw_skystat_batched call that used workspace `ws`, read from it (call on
+ * the same stream, after that call).  out32: total_pix records of 9 + 4 n_ifo
+ * float32 -- energy_array_plus, energy_array_cross, pixel_mask,
+ * gaussian_noise_correction, coherent_energy, p00_POL radius and angle,
+ * p90_POL radius and angle, noise_amplitude_00[n_ifo],
+ * noise_amplitude_90[n_ifo], f[n_ifo], F[n_ifo] (the dominant-polarisation
+ * antenna vectors); out64: total_pix records of 4 n_ifo float64 -- pd, pD,
+ * ps, pS (the data and signal packets).  The inputs of the reference's
+ * populate_detection_statistics (detection_statistics.py:31-440). */
+int pgw_skystat_pixel_arrays(int n_ifo, int64_t total_pix, const void* ws, size_t ws_bytes,
+                             float* out32, double* out64, void* stream);
+
 /* Normalised sky probability of selected clusters of a batched sky loop:
  * the reference caller's softmax of the sky-statistic map
  * (pycwb/modules/likelihoodWP/likelihood.py:338-342: p = exp(s - max s) /

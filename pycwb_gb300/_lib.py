@@ -139,6 +139,8 @@ def load():
         L.pgw_sky_loop_noalloc.restype = ctypes.c_int
         L.pgw_sky_loop_noalloc_max_scratch.restype = sz
         L.pgw_sky_probability.argtypes = [i32, i64, P, i64, P, P, P, P]
+        L.pgw_skystat_pixel_arrays.argtypes = [i32, i64, P, sz, P, P, P]
+        L.pgw_skystat_pixel_arrays.restype = ctypes.c_int
         L.pgw_sky_probability.restype = ctypes.c_int
         for name in ("pgw_fp32_fma_peak", "pgw_calculate_dpf", "pgw_scan_sky_for_best_fit", "pgw_sky_loop",
                      "pgw_sky_loop_batched", "pgw_batch_get_td_vecs"):

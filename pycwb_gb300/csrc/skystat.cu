@@ -76,7 +76,8 @@ struct StatArgs {
 template <int I> struct FW {
   static constexpr int v0 = 0, v9 = I, s = 2 * I, Sg = 3 * I, f = 4 * I, F = 5 * I, pd = 6 * I,
                        pD = 7 * I, ps = 8 * I, pS = 9 * I, fp = 10 * I, fx = fp + 1, et = fp + 2,
-                       msk = fp + 3, ec = fp + 4, gn = fp + 5, stride = fp + 6;
+                       msk = fp + 3, ec = fp + 4, gn = fp + 5, ee = fp + 6, EE = fp + 7,
+                       pr0 = fp + 8, pa0 = fp + 9, pr9 = fp + 10, pa9 = fp + 11, stride = fp + 12;
 };
 // double workspace per pixel
 template <int I> struct DW {
@@ -243,6 +244,11 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
     for (int i = 0; i < I; ++i) { a2 = A(a2, M(s[i], s[i])); A2 = A(A2, M(Sg[i], Sg[i])); aA = A(aA, M(s[i], Sg[i])); }
     float osi = M(aA, 2.0f), oco = S(a2, A2);
     const float onn = __fsqrt_rn(A(M(oco, oco), M(osi, osi)));
+    {   // the per-pixel plus / cross energies of the signal (sky_stat.py:279-281)
+      const float eo = A(A(a2, A2), 1e-21f);
+      w[W::ee] = D(A(eo, onn), 2.0f);
+      w[W::EE] = D(S(eo, onn), 2.0f);
+    }
     const float occ = D(oco, A(onn, 1e-21f));
     const float sg = osi > 0.0f ? 1.0f : -1.0f;
     osi = __fsqrt_rn(D(S(1.0f, occ), 2.0f));
@@ -274,6 +280,25 @@ __global__ void __launch_bounds__(kThreads) skystat_kernel(StatArgs a) {
     w[W::fp] = fp; w[W::fx] = fx; w[W::et] = et; w[W::msk] = msk;
     w[W::ec] = M(static_cast<float>(mks), A(ss, SS));
     w[W::gn] = M(static_cast<float>(mks * 2.0), msk);
+    // the network-plane radius and angle of both quadratures (avx_pol_ps,
+    // packet_ops.py:564-655), float64 as the reference's sums
+    {
+      const double mkp = msk > 0.0f ? 1.0 : 0.0;
+      double xp = 0.0, XP = 0.0, xx = 0.0, XX = 0.0;
+      for (int i = 0; i < I; ++i) {
+        const double p0v = static_cast<double>(v0[i]) * mkp, p9v = static_cast<double>(v9[i]) * mkp;
+        xp += static_cast<double>(f[i]) * p0v;
+        XP += static_cast<double>(f[i]) * p9v;
+        xx += static_cast<double>(F[i]) * p0v;
+        XX += static_cast<double>(F[i]) * p9v;
+      }
+      const double o = 1e-9, fpd = fp, fxd = fx;
+      const double sfp = sqrt(fpd) + o, sfx = sqrt(fxd) + o;
+      w[W::pr0] = static_cast<float>(sqrt(xp * xp / (fpd + o) + xx * xx / (fxd + o)));
+      w[W::pa0] = static_cast<float>(atan2(xx / sfx, xp / sfp));
+      w[W::pr9] = static_cast<float>(sqrt(XP * XP / (fpd + o) + XX * XX / (fxd + o)));
+      w[W::pa9] = static_cast<float>(atan2(XX / sfx, XP / sfp));
+    }
   }
   __syncthreads();
 
@@ -589,7 +614,7 @@ cudaError_t launch(const StatArgs& a, int n_clusters, cudaStream_t s) {
 
 extern "C" size_t pgw_skystat_workspace_bytes(int n_ifo, int64_t total_pix) {
   if (n_ifo < 1 || n_ifo > PGW_MAX_IFO || total_pix < 0) return 0;
-  const size_t fl = static_cast<size_t>(10 * n_ifo + 6) * 4;
+  const size_t fl = static_cast<size_t>(10 * n_ifo + 12) * 4;
   const size_t db = static_cast<size_t>(8 * n_ifo + 1) * 8;
   return 256 + static_cast<size_t>(total_pix) * (fl + db) + 256;
 }
@@ -638,5 +663,80 @@ extern "C" int pgw_skystat_batched(int n_ifo, int n_clusters, const int64_t* pix
     default: e = launch<8>(a, n_clusters, s); break;
   }
   if (e != cudaSuccess) return pgw::fail(PGW_ERR_CUDA, std::string("skystat_kernel: ") + cudaGetErrorString(e));
+  return PGW_OK;
+}
+
+// ----------------------------------------------------------------------------
+// The per-pixel arrays of the reference's SkyStatistics, from the workspace of
+// the last pgw_skystat_batched call (sky_statistics.py:264-292).
+// ----------------------------------------------------------------------------
+namespace {
+
+template <int I>
+__global__ void skystat_pixels_kernel(int64_t total_pix, const float* __restrict__ wf,
+                                      const double* __restrict__ wd, float* __restrict__ out32,
+                                      double* __restrict__ out64) {
+  using W = FW<I>;
+  using Q = DW<I>;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= total_pix) return;
+  const float* w = wf + p * W::stride;
+  const double* d = wd + p * Q::stride;
+  constexpr int NF = 9 + 4 * I;
+  float* o = out32 + p * NF;
+  o[0] = w[W::ee];
+  o[1] = w[W::EE];
+  o[2] = w[W::msk];
+  o[3] = w[W::gn];
+  o[4] = w[W::ec];
+  o[5] = w[W::pr0];
+  o[6] = w[W::pa0];
+  o[7] = w[W::pr9];
+  o[8] = w[W::pa9];
+  for (int i = 0; i < I; ++i) {
+    o[9 + i] = w[W::ps + i];           // null packet, 00 (the slots hold it after phase 5)
+    o[9 + I + i] = w[W::pS + i];       // null packet, 90
+    o[9 + 2 * I + i] = w[W::f + i];
+    o[9 + 3 * I + i] = w[W::F + i];
+  }
+  double* o64 = out64 + p * (4 * I);
+  for (int i = 0; i < I; ++i) {
+    o64[i] = d[Q::pdd + i];
+    o64[I + i] = d[Q::pDd + i];
+    o64[2 * I + i] = d[Q::psd + i];
+    o64[3 * I + i] = d[Q::pSd + i];
+  }
+}
+
+}  // namespace
+
+extern "C" int pgw_skystat_pixel_arrays(int n_ifo, int64_t total_pix, const void* ws,
+                                        size_t ws_bytes, float* out32, double* out64,
+                                        void* stream) {
+  if (n_ifo < 2 || n_ifo > PGW_MAX_IFO || total_pix < 0)
+    return pgw::fail(PGW_ERR_BAD_SHAPE, "n_ifo must be in [2, 8] and total_pix >= 0");
+  if (total_pix == 0) return PGW_OK;
+  if (!ws || !out32 || !out64) return pgw::fail(PGW_ERR_BAD_ARGUMENT, "NULL device pointer");
+  if (ws_bytes < pgw_skystat_workspace_bytes(n_ifo, total_pix))
+    return pgw::fail(PGW_ERR_WORKSPACE, "workspace smaller than pgw_skystat_workspace_bytes");
+  const char* base = static_cast<const char*>(ws);
+  const uintptr_t al = (reinterpret_cast<uintptr_t>(base) + 255) & ~static_cast<uintptr_t>(255);
+  const char* b = reinterpret_cast<const char*>(al);
+  const double* wd = reinterpret_cast<const double*>(b);
+  const float* wf = reinterpret_cast<const float*>(b + static_cast<size_t>(8 * n_ifo + 1) * 8 *
+                                                          static_cast<size_t>(total_pix));
+  const unsigned blocks = static_cast<unsigned>((total_pix + 255) / 256);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (n_ifo) {
+    case 2: skystat_pixels_kernel<2><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    case 3: skystat_pixels_kernel<3><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    case 4: skystat_pixels_kernel<4><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    case 5: skystat_pixels_kernel<5><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    case 6: skystat_pixels_kernel<6><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    case 7: skystat_pixels_kernel<7><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+    default: skystat_pixels_kernel<8><<<blocks, 256, 0, s>>>(total_pix, wf, wd, out32, out64); break;
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return pgw::fail(PGW_ERR_CUDA, std::string("skystat_pixels_kernel: ") + cudaGetErrorString(e));
   return PGW_OK;
 }

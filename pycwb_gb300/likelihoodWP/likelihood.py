@@ -25,7 +25,8 @@ update_chirp_mass_statistics and compute_sky_error_region (:389-418) -- is
 not part of this path.  ``post`` takes it: a callable
 ``post(cluster, sky_statistics, skymap_statistics, context)`` run on every
 accepted cluster; ``post=reference_post_processing`` calls the reference's
-own functions when the pycwb package is importable.
+own functions when the pycwb package is importable, on the GPU statistics
+(their per-pixel arrays come back for the accepted clusters only).
 
 Inputs are the reference's objects, read by attribute: a cluster has
 ``pixel_arrays`` (``noise_rms`` (nIFO, P), ``td_amp_dense()`` (P, nIFO,
@@ -230,7 +231,8 @@ def _run_group(setup, jobs, big, valid, xgb_rho_mode):
     t_prob = time.perf_counter() - t1
     t2 = time.perf_counter()
     xt, lk = pack_xtalk([(j.xtalk_rows, j.xtalk_lookup) for j in jobs])
-    stats = statistics_batched(loop, res.l_max, xt, lk, xgb_rho_mode=xgb_rho_mode)
+    stats, pixels = statistics_batched(loop, res.l_max, xt, lk, xgb_rho_mode=xgb_rho_mode,
+                                       pixel_arrays=keep)
     t_stat = time.perf_counter() - t2
     cls = _skymap_class()
     n_ifo = tables.n_ifo
@@ -248,7 +250,7 @@ def _run_group(setup, jobs, big, valid, xgb_rho_mode):
                            "probability_sum": float(summary[k, 1]),
                            "directions_50": int(summary[k, 2]) if summary[k, 2] == summary[k, 2] else -1,
                            "directions_90": int(summary[k, 3]) if summary[k, 3] == summary[k, 3] else -1}
-        out[c] = (sm, SkyStatistics.from_record(stats[c], n_ifo))
+        out[c] = (sm, SkyStatistics.from_record(stats[c], n_ifo, pixels[c]))
     return out
 
 
@@ -319,32 +321,16 @@ def _finish(nIFO, job, skymap, stats, config, setup, post, context):
 
 def reference_post_processing(cluster, sky_statistics, skymap_statistics, context):
     """The reference's host post-processing of an accepted cluster
-    (likelihood.py:389-418): populate_detection_statistics,
-    update_chirp_mass_statistics and compute_sky_error_region from the
-    installed pycwb package.  populate_detection_statistics reads the
-    per-pixel arrays of the reference's SkyStatistics (packets, masks), which
-    the GPU statistics do not return; they are recomputed here for this one
-    cluster by the reference's compute_statistics_at_sky_position."""
+    (likelihood.py:389-418) from the installed pycwb package:
+    populate_detection_statistics on the GPU statistics at the maximum (its
+    scalars and per-pixel arrays: packets, masks, noise amplitudes),
+    update_chirp_mass_statistics and compute_sky_error_region."""
     from pycwb.modules.likelihoodWP import detection_statistics as ds
-    from pycwb.modules.likelihoodWP.sky_statistics import compute_statistics_at_sky_position
-    from pycwb.modules.likelihoodWP.pixel_data import extract_pixel_time_delay_data as ext
     from pycwb.modules.reconstruction.getMRAwaveform import _create_wdm_set_python
 
     config, setup, nIFO = context["config"], context["setup"], context["nIFO"]
-    big = is_big_cluster(config, setup, len(cluster.pixel_arrays))
-    ml, FP_t, FX_t, _, _, _ = _grid(setup, big)
-    w, t0, t9, _ = ext(None, nIFO, pixel_arrays=cluster.pixel_arrays)
-    t0 = np.transpose(t0.astype(np.float32), (2, 0, 1))
-    t9 = np.transpose(t9.astype(np.float32), (2, 0, 1))
-    REG = np.array([setup["delta_regulator"] * np.sqrt(2), skymap_statistics.regulator, 0.0],
-                   dtype=np.float32)
-    full = compute_statistics_at_sky_position(
-        skymap_statistics.l_max, nIFO, len(cluster.pixel_arrays), FP_t, FX_t,
-        w.T.astype(np.float32), t0, t9, ml, REG, setup["network_energy_threshold"],
-        context["cluster_xtalk"], context["cluster_xtalk_lookup"],
-        xgb_rho_mode=setup["xgb_rho_mode"])
     ds.populate_detection_statistics(
-        full, skymap_statistics, cluster=cluster, n_ifo=nIFO, xtalk=context["xtalk"],
+        sky_statistics, skymap_statistics, cluster=cluster, n_ifo=nIFO, xtalk=context["xtalk"],
         network_energy_threshold=setup["network_energy_threshold"],
         xgb_rho_mode=setup["xgb_rho_mode"], config=config,
         cluster_xtalk=context["cluster_xtalk"], cluster_xtalk_lookup=context["cluster_xtalk_lookup"],

@@ -2,11 +2,14 @@
 
 Drop-in for pycwb/modules/likelihoodWP/sky_statistics.py:26-262
 (compute_statistics_at_sky_position, legacy name calculate_sky_statistics):
-the same arguments, returning the event statistics of SkyStatistics (the
-scalars Gn, Ec, Dc, Rc, Eh, Es, Np, Em, Lm, norm, cc, rho, xrho, Lo, Eo,
-N_pix_effective and the per-detector signal SNR S_snr).  The per-pixel
-arrays of the reference's SkyStatistics (packets, masks, polar maps) stay
-on the device and are not returned.
+the same arguments, returning SkyStatistics: the scalars Gn, Ec, Dc, Rc, Eh,
+Es, Np, Em, Lm, norm, cc, rho, xrho, Lo, Eo, N_pix_effective, the
+per-detector signal SNR S_snr, and the per-pixel arrays the reference's
+populate_detection_statistics reads (energy_array_plus/cross, pixel_mask,
+gaussian_noise_correction, coherent_energy, noise_amplitude_00/90, the
+packets pd, pD, ps, pS, the antenna vectors f, F and the polar maps
+p00_POL, p90_POL as (2, P) rows of radius and angle), from
+pgw_skystat_pixel_arrays.
 
 ``statistics_batched`` evaluates every cluster of a BatchedSkyLoop at its
 sky maximum in one launch, straight from the loop's device inputs.
@@ -58,12 +61,49 @@ class SkyStatistics:
     Eo: np.float32
     N_pix_effective: float
     S_snr: np.ndarray
+    # per-pixel arrays (None unless asked for): the reference's names and shapes
+    energy_array_plus: np.ndarray = None
+    energy_array_cross: np.ndarray = None
+    pixel_mask: np.ndarray = None
+    gaussian_noise_correction: np.ndarray = None
+    coherent_energy: np.ndarray = None
+    noise_amplitude_00: np.ndarray = None
+    noise_amplitude_90: np.ndarray = None
+    pd: np.ndarray = None
+    pD: np.ndarray = None
+    ps: np.ndarray = None
+    pS: np.ndarray = None
+    f: np.ndarray = None
+    F: np.ndarray = None
+    p00_POL: np.ndarray = None
+    p90_POL: np.ndarray = None
 
     @classmethod
-    def from_record(cls, r, n_ifo):
+    def from_record(cls, r, n_ifo, pixels=None):
         return cls(**{k: np.float32(r[k]) for k in SKYSTAT_SCALARS},
                    N_pix_effective=float(r["N_pix_effective"]),
-                   S_snr=np.array(r["S_snr"][:n_ifo], dtype=np.float64))
+                   S_snr=np.array(r["S_snr"][:n_ifo], dtype=np.float64), **(pixels or {}))
+
+
+def split_pixel_arrays(out32, out64, n_ifo, pix_offsets):
+    """Per cluster, the reference's per-pixel SkyStatistics arrays from the
+    records of pgw_skystat_pixel_arrays: a dict of numpy arrays with the
+    reference's names and shapes ((P,), (n_ifo, P) or (P, n_ifo))."""
+    I = int(n_ifo)
+    out = []
+    for c in range(len(pix_offsets) - 1):
+        a, b = int(pix_offsets[c]), int(pix_offsets[c + 1])
+        r32, r64 = out32[a:b], out64[a:b]
+        out.append(dict(
+            energy_array_plus=r32[:, 0].copy(), energy_array_cross=r32[:, 1].copy(),
+            pixel_mask=r32[:, 2].copy(), gaussian_noise_correction=r32[:, 3].copy(),
+            coherent_energy=r32[:, 4].copy(),
+            p00_POL=np.stack([r32[:, 5], r32[:, 6]]), p90_POL=np.stack([r32[:, 7], r32[:, 8]]),
+            noise_amplitude_00=r32[:, 9:9 + I].T.copy(), noise_amplitude_90=r32[:, 9 + I:9 + 2 * I].T.copy(),
+            f=r32[:, 9 + 2 * I:9 + 3 * I].copy(), F=r32[:, 9 + 3 * I:9 + 4 * I].copy(),
+            pd=r64[:, :I].T.copy(), pD=r64[:, I:2 * I].T.copy(),
+            ps=r64[:, 2 * I:3 * I].T.copy(), pS=r64[:, 3 * I:4 * I].T.copy()))
+    return out
 
 
 def pack_xtalk(per_cluster):
@@ -82,7 +122,7 @@ def pack_xtalk(per_cluster):
 
 
 def _run(n_ifo, pix_off, td_off, total_pix, FP, FX, rms, td00, td90, n_delay, ml, sky_idx, regs,
-         REG0, ethr, xtalk, lookup, xgb, stream):
+         REG0, ethr, xtalk, lookup, xgb, stream, pixel_arrays=False):
     L = _lib.load()
     dev = FP.device
     n = int(sky_idx.numel())
@@ -104,6 +144,15 @@ def _run(n_ifo, pix_off, td_off, total_pix, FP, FX, rms, td00, td90, n_delay, ml
         int(bool(xgb)), P(ws),
         ws.numel(), P(out), ctypes.c_void_p(stream.cuda_stream))
     _lib.check(rc, "pgw_skystat_batched")
+    pix = None
+    if pixel_arrays is not False and total_pix > 0:
+        with torch.cuda.stream(stream):
+            o32 = torch.empty((total_pix, 9 + 4 * n_ifo), dtype=torch.float32, device=dev)
+            o64 = torch.empty((total_pix, 4 * n_ifo), dtype=torch.float64, device=dev)
+        rc = L.pgw_skystat_pixel_arrays(n_ifo, total_pix, P(ws), ws.numel(), P(o32), P(o64),
+                                        ctypes.c_void_p(stream.cuda_stream))
+        _lib.check(rc, "pgw_skystat_pixel_arrays")
+        pix = (o32, o64)
     stream.synchronize()
     res = np.frombuffer(out.cpu().numpy().tobytes(), dtype=SKYSTAT_DTYPE).copy()
     bad = res["status"] != 0
@@ -112,15 +161,34 @@ def _run(n_ifo, pix_off, td_off, total_pix, FP, FX, rms, td00, td90, n_delay, ml
         raise RuntimeError(f"pgw_skystat_batched: cluster status {codes} "
                            f"({_lib.STATUS_NAMES.get(codes[0], codes[0])}) for "
                            f"{int(bad.sum())} clusters")
+    if pixel_arrays is not False:
+        offs = pix_off.cpu().numpy()
+        n = len(offs) - 1
+        want = range(n) if pixel_arrays is True else sorted(set(int(c) for c in pixel_arrays))
+        arrays = [None] * n
+        for c in want:             # only the wanted clusters' pixels leave the device
+            a, b = int(offs[c]), int(offs[c + 1])
+            if pix is None or b == a:
+                arrays[c] = split_pixel_arrays(np.zeros((0, 9 + 4 * n_ifo), np.float32),
+                                               np.zeros((0, 4 * n_ifo)), n_ifo, [0, 0])[0]
+                continue
+            with torch.cuda.stream(stream):
+                r32, r64 = pix[0][a:b].cpu().numpy(), pix[1][a:b].cpu().numpy()
+            arrays[c] = split_pixel_arrays(r32, r64, n_ifo, [0, b - a])[0]
+        return res, arrays
     return res
 
 
 def statistics_batched(loop, l_max, xtalk, xtalk_lookup, *, regulators=None,
-                       xgb_rho_mode=False):
+                       xgb_rho_mode=False, pixel_arrays=False):
     """Statistics of every cluster of a BatchedSkyLoop at its sky maximum
     (l_max, e.g. BatchResult.l_max), from the loop's device inputs.
     regulators: REG[1] per cluster (default: the loop's last regulators).
-    Returns a structured array of SKYSTAT_DTYPE, one record per cluster."""
+    Returns a structured array of SKYSTAT_DTYPE, one record per cluster; with
+    pixel_arrays (True for every cluster, or a sequence of cluster indices)
+    also a list with, per cluster, a dict of the reference's per-pixel
+    SkyStatistics arrays (split_pixel_arrays), None for clusters not asked
+    for -- only their pixels are copied to the host."""
     t, b = loop.t, loop.b
     n = b.n_clusters
     dev = loop.td00.device
@@ -136,7 +204,8 @@ def statistics_batched(loop, l_max, xtalk, xtalk_lookup, *, regulators=None,
         raise ValueError(f"regulators needs one value per cluster ({n})")
     return _run(t.n_ifo, loop.pix_off, loop.td_off, b.total_pix, t.FP, t.FX, loop.rms, loop.td00,
                 loop.td90, b.n_delay, t.ml, l, regs.contiguous(), t.REG0,
-                t.network_energy_threshold, xtalk, xtalk_lookup, xgb_rho_mode, loop.stream)
+                t.network_energy_threshold, xtalk, xtalk_lookup, xgb_rho_mode, loop.stream,
+                pixel_arrays=pixel_arrays)
 
 
 def compute_statistics_at_sky_position(sky_idx, n_ifo, n_pix, FP, FX, rms, td00, td90, ml, REG,
@@ -175,8 +244,9 @@ def compute_statistics_at_sky_position(sky_idx, n_ifo, n_pix, FP, FX, rms, td00,
     res = _run(n_ifo, pix_off, td_off, n_pix, FP_d, FX_d, rms_d, td00_d, td90_d,
                int(td00_d.shape[0]), ml_d, l, regs, float(REG[0]),
                float(np.float32(network_energy_threshold)), cluster_xtalk,
-               cluster_xtalk_lookup_table, xgb_rho_mode, s)
-    return SkyStatistics.from_record(res[0], n_ifo)
+               cluster_xtalk_lookup_table, xgb_rho_mode, s, pixel_arrays=True)
+    res, pix = res
+    return SkyStatistics.from_record(res[0], n_ifo, pix[0])
 
 
 calculate_sky_statistics = compute_statistics_at_sky_position
