@@ -353,6 +353,8 @@ def main():
                     help="with --profile: the WDM transform field only")
     ap.add_argument("--profile-regulator", action="store_true",
                     help="with --profile: one regulator-only launch instead")
+    ap.add_argument("--profile-plain", action="store_true",
+                    help="with --profile: one plain pgw_sky_loop call per size of PLAIN_SIZES")
     ap.add_argument("--profile", action="store_true",
                     help="one eager launch of the batched loop and exit (for ncu)")
     args = ap.parse_args()
@@ -437,6 +439,10 @@ def main():
     assert n_sky == n_sky_expected
     tables = SkyTables.from_arrays(FP_t, FX_t, ml, None, **{k: reg[k] for k in (
         "network_energy_threshold", "gamma_regulator", "delta_regulator", "netCC")})
+    if args.profile and args.profile_plain:
+        time_plain_sizes(L, tables, ml, FP_t, FX_t, dev, args.seed, reps=0)
+        print(json.dumps({"profile": "one plain call per size", "sizes": PLAIN_SIZES}))
+        return
 
     rng = np.random.default_rng(args.seed + 1000 * rank)
     sizes = log_uniform_sizes(rng, args.clusters, 20, 3000)
@@ -576,6 +582,7 @@ def main():
     plain = None
     if not args.no_plain:
         plain = time_plain(L, loop, tables, batch, shape, dev)
+        plain["us_per_call_by_size"] = time_plain_sizes(L, tables, ml, FP_t, FX_t, dev, args.seed)
         plain["value"] = world * work_evals / (plain["ms"] * 1e-3)
         plain["roofline_frac"] = (useful_ops / (plain["ms"] * 1e-3) / 1e12 / peak) if peak else None
 
@@ -1138,6 +1145,65 @@ def time_plain(L, loop, tables, batch, shape, dev):
     return {"ms": ms, "launches": batch.n_clusters * 2,  # set-up, sky loop
             "note": "same kernel, one pgw_sky_loop per cluster with the default one-cluster "
                     "launch shape, device-resident, 1 timed pass"}
+
+
+PLAIN_SIZES = (20, 100, 300, 1000, 3000)
+
+
+def time_plain_sizes(L, tables, ml, FP_t, FX_t, dev, seed, reps=50):
+    """One cluster of each size in PLAIN_SIZES (SNR 20), pgw_sky_loop over the
+    whole sky with device-resident inputs: microseconds per call, CUDA events
+    over `reps` calls after 5 warm-up calls.  reps = 0: one call per size,
+    untimed (the form an ncu capture runs)."""
+    import torch
+
+    from pycwb_gb300.synthetic import make_cluster
+
+    rng = np.random.default_rng(seed + 77)
+    n_sky = tables.n_sky
+    s = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(s):
+        st = torch.empty((11, n_sky), dtype=torch.float32, device=dev)
+        res = torch.empty(32, dtype=torch.uint8, device=dev)
+        regs = torch.empty(1, dtype=torch.float64, device=dev)
+    out = {}
+    for P in PLAIN_SIZES:
+        td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, P, K_TD, 20.0)
+        with torch.cuda.stream(s):
+            d0 = torch.from_numpy(td00).to(dev)
+            d9 = torch.from_numpy(td90).to(dev)
+            rm = torch.from_numpy(rms).to(dev)
+            ws = torch.empty(int(L.pgw_workspace_bytes(len(IFOS), 2 * K_TD + 1, P, 1)),
+                             dtype=torch.uint8, device=dev)
+
+        def one():
+            rc = L.pgw_sky_loop(len(IFOS), P, n_sky, tables.FP.data_ptr(), tables.FX.data_ptr(),
+                                rm.data_ptr(), d0.data_ptr(), d9.data_ptr(), 2 * K_TD + 1,
+                                tables.ml.data_ptr(), tables.REG0, tables.gamma_regulator,
+                                tables.netCC, tables.network_energy_threshold,
+                                tables.valid.data_ptr(), tables.valid.numel(),
+                                tables.order.data_ptr(), tables.reg_order.data_ptr(),
+                                st.data_ptr(), res.data_ptr(), regs.data_ptr(), None,
+                                ws.data_ptr(), ws.numel(), s.cuda_stream)
+            if rc:
+                raise RuntimeError(L.pgw_last_error().decode())
+
+        if reps == 0:
+            one()
+            s.synchronize()
+            continue
+        for _ in range(5):
+            one()
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            one()
+        e1.record(s)
+        e1.synchronize()
+        out[str(P)] = round(e0.elapsed_time(e1) * 1e3 / reps, 1)
+    return out
 
 
 if __name__ == "__main__":
