@@ -126,14 +126,16 @@ int pgw_scan_sky_for_best_fit(int n_ifo, int64_t n_pix, int64_t n_sky, const flo
  *   stages         chunks in flight per CTA, 2..4
  *   min_blocks     occupancy target the kernel is compiled for: 3 or 4 CTAs
  *                  per SM for n_ifo <= 4, 2 above
- *   fast_math      0 (automatic) or 1: the scan's divisions are a
- *                  reciprocal estimate with one correction step (Markstein;
- *                  within one ulp of the correctly rounded quotient, no
- *                  slow-path branch) and its square roots sqrt.approx.f32,
- *                  except the packet-rotation norm, refined likewise; -1:
- *                  IEEE rounding of every division and square root.  Both meet the 1e-4 relative
- *                  parity bar; the regulator's decisions are exact either way
- *                  (its fallback always uses IEEE arithmetic). */
+ *   fast_math      0 (automatic) or 1: the scan's two rotation quotients
+ *                  are a reciprocal estimate with one correction step
+ *                  (Markstein; within one ulp of the correctly rounded
+ *                  quotient, no slow-path branch), its other ten quotients
+ *                  the estimate's product (about 2 ulp), its square roots
+ *                  sqrt.approx.ftz.f32 except the packet-rotation norm,
+ *                  refined likewise; -1: IEEE rounding of every division
+ *                  and square root.  Both meet the 1e-4 relative parity
+ *                  bar; the regulator's decisions are exact either way (its
+ *                  fallback always uses IEEE arithmetic). */
 typedef struct {
   int threads;
   int lanes_per_sky;
