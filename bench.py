@@ -1095,8 +1095,10 @@ def time_skystat(loop, res, batch, dev, seed, reps=3):
             "status_ok": int((rec["status"] == 0).sum()),
             "probability_ms": prob_ms, "probability_maps": n_p,
             "probability_note": "pgw_sky_probability: softmax of nSkyStat (float32-accurate "
-                                "exponentials, float64 sum) and the 50 % / 90 % direction counts "
-                                "of every cluster with sky_stat_max > 0, one launch"}
+                                "exponentials, compensated sum, float64 across the block) and "
+                                "the 50 % / 90 % direction counts (binade histogram, bisection "
+                                "in shared memory) of every cluster with sky_stat_max > 0, one "
+                                "launch"}
 
 
 def time_plain(L, loop, tables, batch, shape, dev):
