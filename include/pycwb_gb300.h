@@ -410,7 +410,9 @@ int pgw_skystat_pixel_arrays(int n_ifo, int64_t total_pix, const void* ws, size_
  * the reference caller's softmax of the sky-statistic map
  * (pycwb/modules/likelihoodWP/likelihood.py:338-342: p = exp(s - max s) /
  * sum exp(s - max s) over all n_sky entries, float64 arithmetic, float32
- * result), computed where the maps already are.  stats: the loop's
+ * result), computed where the maps already are, each probability within a
+ * few float32 ulp of the reference's (float32-accurate exponentials, a
+ * compensated sum carried to float64).  stats: the loop's
  * out_stats, cluster c's (11, n_sky) block at c * stats_stride floats;
  * clusters: n_select cluster indices (device int32), or NULL for clusters
  * 0..n_select-1; out_probability: (n_select, n_sky) float32.  out_summary
