@@ -12,12 +12,15 @@ big-cluster switch bBB (a cluster with more than nRES * (precision mod
 the cluster's time (:287-294), rejection of an empty mask; then, for all
 clusters at once, the GPU: one batched launch of the regulator and sky scan
 per distinct (grid, sky mask) -- REG[1] and the 11 sky maps of every
-cluster -- the rejection of sky_stat_max <= 0 (:328-336), the normalised sky
-probability (softmax of nSkyStat, :338-342, pgw_sky_probability) and the
-statistics at each sky maximum (:354-363, pgw_skystat_batched); then, on
-the host, the threshold cut (get_likelihood_rejection_reason, :367-386) and
-the sky-localisation fields of the cluster (:420-432).  Only accepted
-clusters' maps leave the device.
+cluster -- the rejection of sky_stat_max <= 0 (:328-336), the statistics at
+each sky maximum (:354-363, pgw_skystat_batched), the threshold cut on them
+(get_likelihood_rejection_reason, :367-386) and, for the clusters it
+accepts, the normalised sky probability (softmax of nSkyStat, :338-342,
+pgw_sky_probability); then, on the host, the sky-localisation fields of the
+cluster (:420-432).  Only accepted clusters' maps, probabilities and
+per-pixel statistics leave the device; the reference computes the
+probability of every cluster with sky_stat_max > 0, but a rejected
+cluster's result is (None, None) either way.
 
 The reference's remaining host post-processing of an accepted cluster --
 populate_detection_statistics (waveform reconstruction, hrss),
@@ -226,16 +229,38 @@ def _run_group(setup, jobs, big, valid, xgb_rho_mode):
     out = [(None, None)] * len(jobs)
     if keep.size == 0:
         return out
-    t1 = time.perf_counter()
-    prob, summary = sky_probability(loop, keep)
-    t_prob = time.perf_counter() - t1
+    n_ifo = tables.n_ifo
+    # The threshold cut (likelihood.py:367-386) on the statistics at l_max,
+    # before anything per direction or per pixel leaves the device: the
+    # maps, probabilities and per-pixel arrays are read back for the
+    # clusters it accepts only; a rejected cluster comes back as
+    # (None, reason).
+    reasons = {}
+
+    def accepted(records):
+        for c in keep:
+            why = get_likelihood_rejection_reason(
+                SkyStatistics.from_record(records[c], n_ifo), setup["network_energy_threshold"],
+                setup["netEC_threshold"], net_rho_threshold=setup["net_rho_threshold"],
+                xgb_rho_mode=xgb_rho_mode)
+            if why:
+                reasons[int(c)] = why
+        return [c for c in keep if int(c) not in reasons]
+
     t2 = time.perf_counter()
     xt, lk = pack_xtalk([(j.xtalk_rows, j.xtalk_lookup) for j in jobs])
     stats, pixels = statistics_batched(loop, res.l_max, xt, lk, xgb_rho_mode=xgb_rho_mode,
-                                       pixel_arrays=keep)
+                                       pixel_arrays=accepted)
     t_stat = time.perf_counter() - t2
+    for c, why in reasons.items():
+        out[c] = (None, why)
+    keep = np.array([c for c in keep if int(c) not in reasons], dtype=np.int64)
+    if keep.size == 0:
+        return out
+    t1 = time.perf_counter()
+    prob, summary = sky_probability(loop, keep)
+    t_prob = time.perf_counter() - t1
     cls = _skymap_class()
-    n_ifo = tables.n_ifo
     with torch.cuda.stream(loop.stream):
         maps = loop.stats[torch.from_numpy(keep).to(loop.stats.device)].cpu().numpy()
     for k, c in enumerate(keep):
@@ -279,7 +304,10 @@ def evaluate_clusters(nIFO, clusters, config, setup, xtalk, nRMS=None, cluster_i
         grp = [jobs[n] for n in members]
         for n, (sm, st) in zip(members, _run_group(setup, grp, big, grp[0].valid, xgb)):
             if sm is None:
-                logger.info("Cluster rejected: non-positive sky_stat_max")
+                if st is None:
+                    logger.info("Cluster rejected: non-positive sky_stat_max")
+                else:
+                    logger.debug("Cluster rejected due to threshold cuts: %s", st)
                 continue
             results[n] = _finish(nIFO, jobs[n], sm, st, config, setup, post, context)
     return results

@@ -164,7 +164,11 @@ def _run(n_ifo, pix_off, td_off, total_pix, FP, FX, rms, td00, td90, n_delay, ml
     if pixel_arrays is not False:
         offs = pix_off.cpu().numpy()
         n = len(offs) - 1
-        want = range(n) if pixel_arrays is True else sorted(set(int(c) for c in pixel_arrays))
+        if pixel_arrays is True:
+            want = range(n)
+        else:
+            sel = pixel_arrays(res) if callable(pixel_arrays) else pixel_arrays
+            want = sorted(set(int(c) for c in sel))
         arrays = [None] * n
         for c in want:             # only the wanted clusters' pixels leave the device
             a, b = int(offs[c]), int(offs[c + 1])
@@ -185,10 +189,11 @@ def statistics_batched(loop, l_max, xtalk, xtalk_lookup, *, regulators=None,
     (l_max, e.g. BatchResult.l_max), from the loop's device inputs.
     regulators: REG[1] per cluster (default: the loop's last regulators).
     Returns a structured array of SKYSTAT_DTYPE, one record per cluster; with
-    pixel_arrays (True for every cluster, or a sequence of cluster indices)
-    also a list with, per cluster, a dict of the reference's per-pixel
-    SkyStatistics arrays (split_pixel_arrays), None for clusters not asked
-    for -- only their pixels are copied to the host."""
+    pixel_arrays (True for every cluster, a sequence of cluster indices, or
+    a function of the records returning such a sequence) also a list with,
+    per cluster, a dict of the reference's per-pixel SkyStatistics arrays
+    (split_pixel_arrays), None for clusters not asked for -- only their
+    pixels are copied to the host."""
     t, b = loop.t, loop.b
     n = b.n_clusters
     dev = loop.td00.device
