@@ -341,6 +341,9 @@ def main():
     ap.add_argument("--no-pipeline", action="store_true",
                     help="skip the 4-detector HEALPix-8 lag pipeline field")
     ap.add_argument("--pipeline-clusters", type=int, default=1024)
+    ap.add_argument("--no-stage", action="store_true",
+                    help="skip the likelihood-stage drop-in field")
+    ap.add_argument("--stage-clusters", type=int, default=256)
     ap.add_argument("--profile-subnet", action="store_true",
                     help="with --profile: the sub-network-cut sky loop field only")
     ap.add_argument("--profile-td", action="store_true",
@@ -602,6 +605,8 @@ def main():
     pipeline = (time_pipeline(dev, args.seed + 1000 * rank, args.pipeline_clusters)
                 if not args.no_pipeline else None)
     subnet = time_subnet(dev, args.seed + 7 + 1000 * rank) if not args.no_subnet else None
+    stage = (time_stage(ml, FP_t, FX_t, args.order, args.seed + 11 + 1000 * rank,
+                        args.stage_clusters) if not args.no_stage else None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -650,6 +655,7 @@ def main():
             "wdm": wdm_field,
             "pipeline": pipeline,
             "subnet": subnet,
+            "stage": stage,
             "parity_sample": parity,
             "selected": {"found": int(found.sum()),
                          "l_max_equals_injected": int(np.sum(l_max == l_true))},
@@ -1147,6 +1153,92 @@ def time_plain(L, loop, tables, batch, shape, dev):
     return {"ms": ms, "launches": batch.n_clusters * 2,  # set-up, sky loop
             "note": "same kernel, one pgw_sky_loop per cluster with the default one-cluster "
                     "launch shape, device-resident, 1 timed pass"}
+
+
+class _StagePixels:
+    """A cluster's pixel arrays as the reference's stage reads them:
+    noise_rms (nIFO, P) and td_amp_dense() (P, nIFO, 2 (2K + 1))."""
+
+    def __init__(self, rms, td00, td90):
+        self.noise_rms = (1.0 / rms.astype(np.float64)).T
+        self._td = np.concatenate([np.transpose(td00, (2, 1, 0)), np.transpose(td90, (2, 1, 0))],
+                                  axis=2)
+
+    def __len__(self):
+        return self.noise_rms.shape[1]
+
+    def td_amp_dense(self):
+        return self._td
+
+
+class _StageXTalk:
+    """Synthetic packed xtalk overlaps per cluster (get_xtalk_pixels)."""
+
+    def __init__(self):
+        self.by_id = {}
+
+    def get_xtalk_pixels(self, pixels, check=True):
+        rows, lookup = self.by_id[id(pixels)]
+        return lookup, rows
+
+
+def time_stage(ml, FP_t, FX_t, order, seed, n_clusters, reps=2):
+    """The whole likelihood stage through its drop-in
+    (pycwb_gb300.likelihoodWP.likelihood.likelihood_wrapper, the reference's
+    likelihood.py:58-135 signature) on host cluster objects: per-cluster
+    input extraction on the host, one batched regulator + scan launch, the
+    statistics at every maximum and the threshold cut, the sky probability
+    and the read-back of the accepted clusters' 11 maps, probabilities and
+    per-pixel statistics.  Host wall time per call after one warm-up call;
+    pixel counts log-uniform in [20, 3000], SNR U[8, 40]."""
+    from types import SimpleNamespace
+
+    from pycwb_gb300.likelihoodWP.likelihood import likelihood_wrapper
+    from pycwb_gb300.likelihoodWP.likelihood_setup import prepare_likelihood_inputs
+    from pycwb_gb300.synthetic import log_uniform_sizes, make_cluster
+
+    cfg = SimpleNamespace(nIFO=len(IFOS), Acore=math.sqrt(2.0), gamma=0.5, delta=0.5,
+                          netRHO=3.5, netCC=0.5, healpix=order, precision=0, nRES=1)
+    setup = prepare_likelihood_inputs(cfg, None, len(IFOS), ml=ml, FP=FP_t.T, FX=FX_t.T)
+    rng = np.random.default_rng(seed)
+    sizes = log_uniform_sizes(rng, n_clusters, 20, 3000)
+    xtalk = _StageXTalk()
+    clusters = []
+    for P in sizes:
+        td00, td90, rms, _ = make_cluster(rng, ml, FP_t, FX_t, int(P), K_TD,
+                                          float(rng.uniform(8.0, 40.0)))
+        pix = _StagePixels(rms, td00, td90)
+        xtalk.by_id[id(pix)] = synthetic_xtalk_rows(rng, [int(P)])
+        clusters.append(SimpleNamespace(pixel_arrays=pix, cluster_status=0, cluster_time=5.0,
+                                        cluster_freq=200.0))
+    lag = SimpleNamespace(clusters=clusters)
+
+    def call():
+        for cl in clusters:
+            cl.cluster_status = 0
+            cl.cluster_meta = SimpleNamespace(l_max=None, theta=None, phi=None, c_time=0.0,
+                                              c_freq=0.0)
+        return likelihood_wrapper(cfg, [lag], None, None, xtalk=xtalk, setup=setup)
+
+    call()
+    secs, accepted = [], 0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = call()
+        secs.append(time.perf_counter() - t0)
+        accepted = len(out[0])
+    t = float(np.median(secs))
+    n_sky = int(ml.shape[1])
+    return {"workload": f"{n_clusters} clusters, pixels log-uniform[20,3000], SNR U[8,40], "
+                        f"HEALPix {order}, {len(IFOS)} detectors, synthetic xtalk "
+                        "(5 rows per pixel)",
+            "api": "likelihood_wrapper (likelihood.py:58-135 signature)",
+            "pixels": int(sizes.sum()), "accepted": accepted, "s_per_call": t,
+            "clusters_per_s": n_clusters / t, "cluster_sky_evals_per_s": n_clusters * n_sky / t,
+            "d2h_bytes": accepted * (11 + 1) * 4 * n_sky,
+            "note": "host wall time of the drop-in call: input extraction per cluster, "
+                    "the GPU stage, and the accepted clusters' maps and per-pixel arrays "
+                    "read back"}
 
 
 PLAIN_SIZES = (20, 100, 300, 1000, 3000)

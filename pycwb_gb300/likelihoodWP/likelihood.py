@@ -126,11 +126,26 @@ def _grid(setup, big: bool):
             setup["ra_arr"] if phi is None else phi, setup["dec_arr"] if lat is None else lat)
 
 
-def _tables(setup, big: bool, valid: np.ndarray) -> SkyTables:
+def _mask_digest(valid: np.ndarray, memo: dict | None = None) -> str:
+    """Content digest of a set of valid directions.  Jobs usually share the
+    setup's one array (a mask that does not depend on the event time), so
+    `memo` keeps the digest per live array object: one hash per distinct
+    array instead of one per cluster (1.5 MB per HEALPix-7 sky)."""
+    if memo is not None:
+        hit = memo.get(id(valid))
+        if hit is not None and hit[0] is valid:
+            return hit[1]
+    d = hashlib.sha1(np.ascontiguousarray(valid, np.int64).tobytes()).hexdigest()
+    if memo is not None:
+        memo[id(valid)] = (valid, d)
+    return d
+
+
+def _tables(setup, big: bool, valid: np.ndarray, digest: str | None = None) -> SkyTables:
     """Device sky tables of one (grid, sky mask), kept in the setup dict so
     that later calls of the segment reuse them."""
     cache = setup.setdefault("_gpu_tables_by_mask", {})
-    key = (bool(big), hashlib.sha1(np.ascontiguousarray(valid, np.int64).tobytes()).hexdigest())
+    key = (bool(big), digest if digest is not None else _mask_digest(valid))
     t = cache.get(key)
     if t is None:
         ml, FP_t, FX_t, n_sky, _, _ = _grid(setup, big)
@@ -180,8 +195,11 @@ def sky_probability(loop: BatchedSkyLoop, clusters) -> tuple[np.ndarray, np.ndar
                                          loop.stream.cuda_stream)
     _lib.check(rc, "sky_probability")
     with torch.cuda.stream(loop.stream):
-        p_h, s_h = prob.cpu().numpy(), summ.cpu().numpy()
-    return p_h, s_h
+        p_h = torch.empty(prob.shape, dtype=prob.dtype, pin_memory=True)
+        p_h.copy_(prob, non_blocking=True)
+        s_h = summ.cpu()
+    loop.stream.synchronize()
+    return p_h.numpy(), s_h.numpy()
 
 
 def _prepare_job(nIFO, cluster, config, setup, xtalk, nRMS, cluster_id):
@@ -213,11 +231,11 @@ def _prepare_job(nIFO, cluster, config, setup, xtalk, nRMS, cluster_id):
                 timings={"data_prep": time.perf_counter() - t0})
 
 
-def _run_group(setup, jobs, big, valid, xgb_rho_mode):
+def _run_group(setup, jobs, big, valid, xgb_rho_mode, digest=None):
     """One batched launch for the jobs that share a (grid, sky mask).
     Returns per job (skymap statistics or None, sky statistics or None)."""
     t0 = time.perf_counter()
-    tables = _tables(setup, big, valid)
+    tables = _tables(setup, big, valid, digest)
     batch = ClusterBatch.from_clusters([(j.td00, j.td90, j.rms) for j in jobs])
     loop = BatchedSkyLoop(tables, batch)
     res = loop.run()
@@ -261,8 +279,14 @@ def _run_group(setup, jobs, big, valid, xgb_rho_mode):
     prob, summary = sky_probability(loop, keep)
     t_prob = time.perf_counter() - t1
     cls = _skymap_class()
+    # the accepted clusters' maps into page-locked memory (torch caches the
+    # blocks, so repeated calls do not pay for the page locking again)
     with torch.cuda.stream(loop.stream):
-        maps = loop.stats[torch.from_numpy(keep).to(loop.stats.device)].cpu().numpy()
+        sel = loop.stats[torch.from_numpy(keep).to(loop.stats.device)]
+        host = torch.empty(sel.shape, dtype=sel.dtype, pin_memory=True)
+        host.copy_(sel, non_blocking=True)
+    loop.stream.synchronize()
+    maps = host.numpy()
     for k, c in enumerate(keep):
         sm = cls.from_tuple((int(res.l_max[c]),) + tuple(maps[k, s] for s in range(len(MAP_FIELDS)))
                             + (float(smax[c]),))
@@ -295,14 +319,15 @@ def evaluate_clusters(nIFO, clusters, config, setup, xtalk, nRMS=None, cluster_i
         if job is not None:
             jobs[n] = job
     # one launch per distinct (grid, sky mask)
-    groups = {}
+    groups, memo = {}, {}
     for n, job in jobs.items():
-        key = (job.big, hashlib.sha1(job.valid.tobytes()).hexdigest())
+        key = (job.big, _mask_digest(job.valid, memo))
         groups.setdefault(key, []).append(n)
     xgb = bool(setup["xgb_rho_mode"])
-    for (big, _), members in groups.items():
+    for (big, digest), members in groups.items():
         grp = [jobs[n] for n in members]
-        for n, (sm, st) in zip(members, _run_group(setup, grp, big, grp[0].valid, xgb)):
+        for n, (sm, st) in zip(members, _run_group(setup, grp, big, grp[0].valid, xgb,
+                                                   digest=digest)):
             if sm is None:
                 if st is None:
                     logger.info("Cluster rejected: non-positive sky_stat_max")

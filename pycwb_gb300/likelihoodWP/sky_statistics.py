@@ -170,15 +170,24 @@ def _run(n_ifo, pix_off, td_off, total_pix, FP, FX, rms, td00, td90, n_delay, ml
             sel = pixel_arrays(res) if callable(pixel_arrays) else pixel_arrays
             want = sorted(set(int(c) for c in sel))
         arrays = [None] * n
-        for c in want:             # only the wanted clusters' pixels leave the device
-            a, b = int(offs[c]), int(offs[c + 1])
-            if pix is None or b == a:
-                arrays[c] = split_pixel_arrays(np.zeros((0, 9 + 4 * n_ifo), np.float32),
-                                               np.zeros((0, 4 * n_ifo)), n_ifo, [0, 0])[0]
-                continue
+        # only the wanted clusters' pixels leave the device, gathered there
+        # into one block and copied back in one transfer per record type
+        want = list(want)
+        spans = [(int(offs[c]), int(offs[c + 1])) for c in want]
+        local = np.concatenate([[0], np.cumsum([b - a for a, b in spans])]).astype(np.int64)
+        r32 = np.zeros((0, 9 + 4 * n_ifo), np.float32)
+        r64 = np.zeros((0, 4 * n_ifo))
+        if pix is not None and local[-1] > 0:
+            idx = np.concatenate([np.arange(a, b, dtype=np.int64) for a, b in spans])
             with torch.cuda.stream(stream):
-                r32, r64 = pix[0][a:b].cpu().numpy(), pix[1][a:b].cpu().numpy()
-            arrays[c] = split_pixel_arrays(r32, r64, n_ifo, [0, b - a])[0]
+                di = torch.from_numpy(idx).to(dev)
+                r32 = pix[0].index_select(0, di).cpu().numpy()
+                r64 = pix[1].index_select(0, di).cpu().numpy()
+        for k, c in enumerate(want):
+            arrays[c] = split_pixel_arrays(r32, r64, n_ifo, local[k:k + 2])[0] \
+                if local[k + 1] > local[k] else \
+                split_pixel_arrays(np.zeros((0, 9 + 4 * n_ifo), np.float32),
+                                   np.zeros((0, 4 * n_ifo)), n_ifo, [0, 0])[0]
         return res, arrays
     return res
 

@@ -93,7 +93,7 @@ class _FakeGPU:
     def __init__(self):
         self.launches = []
 
-    def __call__(self, setup, jobs, big, valid, xgb):
+    def __call__(self, setup, jobs, big, valid, xgb, digest=None):
         self.launches.append((big, valid.tolist(), [j.rms.shape[0] for j in jobs]))
         n_sky = setup["n_sky_big_cluster"] if big else setup["n_sky"]
         out = []
