@@ -19,6 +19,10 @@ Reported (one JSON line on rank 0):
               FMA peak of the device
   cpu_baseline  the CPU oracle (a restatement of the reference's loops,
               OpenMP over the sky) on a bounded sample, all host cores
+  skystat, stage, ...  the stage around the loop: the statistics at every
+              maximum and the sky probability (device-timed), and the whole
+              likelihood stage through its drop-in likelihood_wrapper on
+              host cluster objects (host wall time)
 
 --impl reference times the reference's CPU implementation (the oracle port;
 the reference's own compiled code needs numba/ROOT, absent here) on the
