@@ -107,7 +107,7 @@ def _check_cluster(oracle_mod, env, got, reg_gpu, td00, td90, rms, rng, what, fu
 
 
 def test_plain_order7_p1000_whole_sky(sky7, oracle_mod):
-    """Config 2: one 1,000-pixel cluster, SNR 15, every direction of the
+    """One 1,000-pixel cluster, SNR 15, every direction of the
     order-7 sky against the oracle; the selected direction identical."""
     from pycwb_gb300.likelihoodWP import sky_loop
     from pycwb_gb300.synthetic import make_cluster
@@ -142,7 +142,7 @@ def test_plain_order7_p3000(sky7, oracle_mod):
 
 
 def test_batched_order7_size_stratified(sky7, oracle_mod):
-    """Config 3 in miniature: 32 clusters of 20-3,000 pixels (SNR 8-40,
+    """The 4,096-cluster batch in miniature: 32 clusters of 20-3,000 pixels (SNR 8-40,
     independent directions) in one batched launch over the whole order-7 sky."""
     from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch, SkyTables
     from pycwb_gb300.synthetic import make_cluster
@@ -167,7 +167,7 @@ def test_batched_order7_size_stratified(sky7, oracle_mod):
 
 
 def test_plain_order8_four_detectors_wide_window(oracle_mod):
-    """Config 5's sky and detectors: HEALPix 8 (786,432 directions),
+    """The lag pipeline's sky and detectors: HEALPix 8 (786,432 directions),
     L1/H1/V1/K1, K = 67 (135 delays), one 800-pixel cluster: REG[1] equal
     over the whole sky, the maps on a sample plus the maximum's
     neighbourhood, the maximum identical."""
