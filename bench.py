@@ -575,15 +575,23 @@ def main():
     if not args.no_e2e:
         loop.run()  # warm
         barrier(pg)
+        # every step copies its inputs from pinned host memory and reads its
+        # results back; run_many overlaps step k+1's copy with step k's
+        # launch, so only the first copy is exposed (counted in the time)
+        n_e2e = max(2, min(args.steps, 3))
         t0 = time.perf_counter()
-        n_e2e = max(1, min(args.steps, 2))
-        for _ in range(n_e2e):
-            loop.run(upload=True, download=True)
+        for r in loop.run_many([batch] * n_e2e):
+            pass
         dt = (time.perf_counter() - t0) / n_e2e
         dt = max_over_ranks(pg, dt, dev)
+        t1 = time.perf_counter()
+        loop.run(upload=True, download=True)
+        dt_one = max_over_ranks(pg, time.perf_counter() - t1, dev)
         e2e = {"value": world * work_evals / dt, "unit": UNIT,
                "h2d_bytes_per_step": batch.h2d_bytes, "d2h_bytes_per_step": loop.d2h_bytes,
-               "ms_per_step": dt * 1e3, "steps": n_e2e, "api": "BatchedSkyLoop.run"}
+               "ms_per_step": dt * 1e3, "steps": n_e2e, "api": "BatchedSkyLoop.run_many",
+               "run_ms": dt_one * 1e3,
+               "run_note": "one BatchedSkyLoop.run (copy, launch, read-back in sequence)"}
 
     # ---- plain: one launch per cluster on the same device data ------------
     plain = None

@@ -269,6 +269,70 @@ class BatchedSkyLoop:
         self.stream.synchronize()
         return self.results() if download else None
 
+    def run_many(self, batches):
+        """Stream several batches of this loop's shape through it: yields one
+        BatchResult per batch, in order.  Two device input sets alternate;
+        batch k+1's host -> device copy runs on a copy stream (the copy
+        engine, not the SMs) while batch k's launch computes, so every
+        batch's inputs still cross the bus but only the first copy is
+        exposed.  A yielded result's maps are valid until the next item is
+        asked for (the next launch reuses them).  Each batch must be a
+        ClusterBatch with this loop's offsets (the same cluster sizes).  The
+        first copy, which nothing overlaps, goes through the SMs
+        (copy_from_host); the others through the copy engine."""
+        dev = self.td00.device
+        copy_stream = torch.cuda.Stream(device=dev)
+        spare = [(self.td00, self.td90, self.rms)]
+        with torch.cuda.stream(self.stream):
+            spare.append((torch.empty_like(self.td00), torch.empty_like(self.td90),
+                          torch.empty_like(self.rms)))
+
+        def stage(buf, batch, after_queued=False):
+            if (batch.total_pix != self.b.total_pix or batch.n_clusters != self.b.n_clusters
+                    or not np.array_equal(batch.pix_offsets, self.b.pix_offsets)):
+                raise ValueError("run_many: every batch needs this loop's cluster sizes")
+            if after_queued:
+                # the first buffer is the loop's own: work queued on the
+                # loop's stream before this call may still read it.  Later
+                # buffers were last read by a launch that has completed.
+                copy_stream.wait_stream(self.stream)
+            with torch.cuda.stream(copy_stream):
+                for dst, src in zip(buf, (batch.td00, batch.td90, batch.rms)):
+                    if after_queued:
+                        # nothing to overlap with: the SMs copy fastest
+                        copy_from_host(dst, src, copy_stream)
+                    else:
+                        # alongside a launch that holds every SM: the copy engine
+                        dst.copy_(src, non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(copy_stream)
+            return ev
+
+        it = iter(batches)
+        cur = next(it, None)
+        if cur is None:
+            return
+        ready = stage(spare[0], cur, after_queued=True)
+        k = 0
+        own = (self.td00, self.td90, self.rms)
+        try:
+            while cur is not None:
+                buf = spare[k % 2]
+                self.stream.wait_event(ready)
+                self.td00, self.td90, self.rms = buf
+                self.launch()
+                nxt = next(it, None)
+                if nxt is not None:
+                    ready = stage(spare[(k + 1) % 2], nxt)
+                self.download()
+                self.stream.synchronize()
+                yield self.results()
+                cur = nxt
+                k += 1
+        finally:
+            copy_stream.synchronize()
+            self.td00, self.td90, self.rms = own
+
     # -- results -----------------------------------------------------------
     def results(self):
         r = self.res_host.numpy().view(dv.RESULT_DTYPE).reshape(-1)

@@ -217,3 +217,42 @@ def test_many_small_clusters_order_in_workspace(oracle_mod):
         if ref[12] > 0 and int(res.l_max[c]) != ref[0]:     # only a near-tie may differ
             a, b = float(ref[7][int(res.l_max[c])]), float(ref[7][ref[0]])
             assert abs(a - b) <= 1e-5 * abs(b), (c, a, b)
+
+
+def test_run_many_streams_batches_like_run(env):
+    """BatchedSkyLoop.run_many (double-buffered inputs, the next batch's copy
+    overlapping the current launch) gives, batch by batch, the results of
+    run() on each batch alone."""
+    from pycwb_gb300.likelihoodWP.batched import BatchedSkyLoop, ClusterBatch
+    from pycwb_gb300.synthetic import make_cluster
+    e = env
+    rng = np.random.default_rng(77)
+    sizes = [40, 250, 7, 120]
+    batches = []
+    for _ in range(3):
+        cl = []
+        for P in sizes:
+            td00, td90, rms, _ = make_cluster(rng, e["ml"], e["FP_t"], e["FX_t"], P, 20,
+                                              float(rng.uniform(8, 40)))
+            cl.append((td00, td90, rms))
+        batches.append(ClusterBatch.from_clusters(cl))
+    singles = []
+    for b in batches:
+        one = BatchedSkyLoop(e["tables"], b)
+        r = one.run()
+        singles.append((r.l_max.copy(), r.sky_stat_max.copy(), r.regulator.copy(),
+                        r.maps.cpu().numpy()))
+    loop = BatchedSkyLoop(e["tables"], batches[0])
+    got = []
+    for r in loop.run_many(batches):
+        got.append((r.l_max.copy(), r.sky_stat_max.copy(), r.regulator.copy(),
+                    r.maps.cpu().numpy()))
+    assert len(got) == 3
+    for (a, b, c, d), (A, B, C, D) in zip(singles, got):
+        np.testing.assert_array_equal(a, A)
+        np.testing.assert_array_equal(b, B)
+        np.testing.assert_array_equal(c, C)
+        np.testing.assert_array_equal(d, D)
+    # the loop's own buffers are back, and a plain run still works
+    r = loop.run()
+    np.testing.assert_array_equal(r.l_max, singles[0][0])
