@@ -289,14 +289,12 @@ extern "C" int pgw_sky_probability(int n_select, int64_t n_sky, const float* sta
   if (n_select == 0) return PGW_OK;
   if (!stats || !out_probability)
     return pgw::fail(PGW_ERR_BAD_ARGUMENT, "pgw_sky_probability: NULL device pointer");
-  static bool attr_set = false;
-  if (!attr_set) {
-    const cudaError_t ea = cudaFuncSetAttribute(
-        sky_probability_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
-    if (ea != cudaSuccess)
-      return pgw::fail(PGW_ERR_CUDA, std::string("sky_probability_kernel smem: ") + cudaGetErrorString(ea));
-    attr_set = true;
-  }
+  // per device and per call (a few microseconds): callers may use several
+  // devices and threads
+  const cudaError_t ea = cudaFuncSetAttribute(
+      sky_probability_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
+  if (ea != cudaSuccess)
+    return pgw::fail(PGW_ERR_CUDA, std::string("sky_probability_kernel smem: ") + cudaGetErrorString(ea));
   sky_probability_kernel<<<n_select, kThreads, kSmem, static_cast<cudaStream_t>(stream)>>>(
       n_sky, stats, stats_stride, clusters, out_probability, out_summary);
   const cudaError_t e = cudaGetLastError();
