@@ -279,7 +279,9 @@ class BatchedSkyLoop:
         asked for (the next launch reuses them).  Each batch must be a
         ClusterBatch with this loop's offsets (the same cluster sizes).  The
         first copy, which nothing overlaps, goes through the SMs
-        (copy_from_host); the others through the copy engine."""
+        (copy_from_host); the others through the copy engine.  Afterwards
+        the loop's device inputs hold whichever batch was staged into them
+        last: upload() before a further launch()."""
         dev = self.td00.device
         copy_stream = torch.cuda.Stream(device=dev)
         spare = [(self.td00, self.td90, self.rms)]
