@@ -19,9 +19,12 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB_PATH = os.path.join(PKG, "libpycwb_gb300.so")
-SOURCES = ["skyloop.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu",
+# the sky-loop kernel's variants compile in five translation units of their
+# own (skyloop_i*.cu), in parallel with the rest
+SOURCES = ["skyloop.cu", "skyloop_i12.cu", "skyloop_i3.cu", "skyloop_i4.cu", "skyloop_i56.cu",
+           "skyloop_i78.cu", "tdamp.cu", "probe.cu", "adjoint.cu", "subnet.cu", "skytables.cu",
            "wdm.cu", "skystat.cu", "skyprob.cu"]
-HEADERS = ["common.cuh"]
+HEADERS = ["common.cuh", "skyloop_kernel.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 _lock = threading.Lock()
