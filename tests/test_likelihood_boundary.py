@@ -238,3 +238,39 @@ def test_rejection_reason_cases(xgb):
         # default |netRHO| = sqrt(netEC / 2)
         assert get_likelihood_rejection_reason(_stats(rho=3.9), 12.0, 32.0, None, xgb) is not None
         assert get_likelihood_rejection_reason(_stats(rho=4.1), 12.0, 32.0, None, xgb) is None
+
+
+def test_mask_digest_memo():
+    """One digest per live array object (the per-cluster masks of a call
+    usually are the setup's one array), equal digests for equal contents."""
+    v = np.arange(1000, dtype=np.int64)
+    memo = {}
+    d = lk._mask_digest(v, memo)
+    assert memo[id(v)] == (v, d) and lk._mask_digest(v, memo) == d
+    w = v.copy()
+    assert lk._mask_digest(w, memo) == d and len(memo) == 2
+    w2 = v[:-1].copy()
+    assert lk._mask_digest(w2, memo) != d
+    assert lk._mask_digest(v) == d          # without a memo
+
+
+def test_split_pixel_arrays_of_a_gathered_block():
+    """split_pixel_arrays on the records of several clusters gathered into one
+    block: each cluster's arrays come from its own rows, in the reference's
+    shapes."""
+    from pycwb_gb300.likelihoodWP.sky_statistics import split_pixel_arrays
+    I = 3
+    sizes = [4, 0, 7]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    n = int(off[-1])
+    r32 = np.arange(n * (9 + 4 * I), dtype=np.float32).reshape(n, -1)
+    r64 = np.arange(n * 4 * I, dtype=np.float64).reshape(n, -1) + 0.5
+    out = split_pixel_arrays(r32, r64, I, off)
+    assert len(out) == 3
+    a, b, c = out
+    assert a["energy_array_plus"].shape == (4,) and b["pd"].shape == (I, 0)
+    np.testing.assert_array_equal(c["energy_array_plus"], r32[4:11, 0])
+    np.testing.assert_array_equal(c["noise_amplitude_00"], r32[4:11, 9:9 + I].T)
+    np.testing.assert_array_equal(c["f"], r32[4:11, 9 + 2 * I:9 + 3 * I])
+    np.testing.assert_array_equal(c["pS"], r64[4:11, 3 * I:4 * I].T)
+    np.testing.assert_array_equal(a["p90_POL"], np.stack([r32[0:4, 7], r32[0:4, 8]]))
