@@ -130,3 +130,33 @@ def test_skystat_workspace_size_is_pure_host_arithmetic():
     assert L.pgw_skystat_workspace_bytes(3, 0) > 0
     assert L.pgw_skystat_workspace_bytes(0, 10) == 0 and L.pgw_skystat_workspace_bytes(9, 10) == 0
     assert L.pgw_wdm_n_time(1000, 16) == 63 and L.pgw_wdm_n_time(10, 0) == -1
+
+
+def test_probability_and_pixel_arrays_reject_bad_arguments_on_the_host():
+    """pgw_sky_probability and pgw_skystat_pixel_arrays check their shapes
+    and pointers before any CUDA call (and do nothing for empty inputs), so
+    the error paths run without a GPU."""
+    from pycwb_gb300 import _lib
+    try:
+        _lib.build()
+    except (RuntimeError, FileNotFoundError) as e:
+        pytest.skip(f"nvcc unavailable: {e}")
+    L = _lib.load()
+    ok = 0
+    # n_select < 0, n_sky < 1, stride below 11 n_sky
+    assert L.pgw_sky_probability(-1, 100, None, 1100, None, None, None, None) != 0
+    assert L.pgw_sky_probability(2, 0, None, 1100, None, None, None, None) != 0
+    assert L.pgw_sky_probability(2, 100, None, 1099, None, None, None, None) != 0
+    # nothing selected: nothing to do
+    assert L.pgw_sky_probability(0, 100, None, 1100, None, None, None, None) == ok
+    # NULL device pointers
+    assert L.pgw_sky_probability(2, 100, None, 1100, None, None, None, None) != 0
+    assert "NULL" in L.pgw_last_error().decode()
+    # per-pixel arrays: detector count, empty input, NULL pointers, workspace size
+    assert L.pgw_skystat_pixel_arrays(1, 10, None, 0, None, None, None) != 0
+    assert L.pgw_skystat_pixel_arrays(3, 0, None, 0, None, None, None) == ok
+    assert L.pgw_skystat_pixel_arrays(3, 10, None, 0, None, None, None) != 0
+    buf = ctypes.create_string_buffer(64)
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    assert L.pgw_skystat_pixel_arrays(3, 10, p, 64, p, p, None) != 0
+    assert "workspace" in L.pgw_last_error().decode()
