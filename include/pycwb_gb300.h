@@ -92,6 +92,16 @@ int pgw_sky_order(const int32_t* ml, int n_ifo, int64_t n_sky, const int64_t* sk
 int pgw_regulator_order(const float* FP, const float* FX, int n_ifo, int64_t n_sky,
                         const int64_t* sky_valid_indices, int64_t n_valid, int32_t* out_order);
 
+/* The same sort, with the sorted directions taken in groups of 32 (one
+ * regulator tile, or two) ordered by their distance from the group where
+ * the mean term crosses the pass threshold gamma_regulator^2: the
+ * directions near it decide last, so their tiles run longest, and taking
+ * them first keeps a launch's last tiles short (longest processing time
+ * first).  Results do not depend on it either. */
+int pgw_regulator_order_lpt(const float* FP, const float* FX, int n_ifo, int64_t n_sky,
+                            const int64_t* sky_valid_indices, int64_t n_valid,
+                            double gamma_regulator, int32_t* out_order);
+
 /* DPF regulator: REG[1] = (n_valid^2 / (n_pass^2 + 1e-9) - 1) * E_thr, where
  * n_pass counts valid directions whose DPF quality sqrt(NI / (NN + 0.01))
  * exceeds gamma_regulator.

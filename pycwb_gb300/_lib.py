@@ -105,6 +105,9 @@ def load():
         L.pgw_sky_order.argtypes = [P, i32, i64, P, i64, P, P]
         L.pgw_regulator_order.argtypes = [P, P, i32, i64, P, i64, P]
         L.pgw_regulator_order.restype = ctypes.c_int
+        if hasattr(L, "pgw_regulator_order_lpt"):
+            L.pgw_regulator_order_lpt.argtypes = [P, P, i32, i64, P, i64, f64, P]
+            L.pgw_regulator_order_lpt.restype = ctypes.c_int
         L.pgw_td_vecs_to_clusters.argtypes = [P, i64, P, P, i32, P, P, i32, i32, P, P, i64, P, P, P, i32,
                                               i32, i32, i32, P, P, P]
         L.pgw_td_vecs_to_clusters.restype = ctypes.c_int
@@ -176,8 +179,10 @@ def sky_order(ml, sky_valid_indices):
     return out, int(n_t.value)
 
 
-def regulator_order(FP_t, FX_t, sky_valid_indices):
-    """Regulator order of the valid directions (host int32), pgw_regulator_order."""
+def regulator_order(FP_t, FX_t, sky_valid_indices, gamma_regulator=None):
+    """Regulator order of the valid directions (host int32): pgw_regulator_order,
+    or with gamma_regulator its longest-tiles-first grouping
+    (pgw_regulator_order_lpt)."""
     import numpy as np
     FP_t = np.ascontiguousarray(FP_t, dtype=np.float32)
     FX_t = np.ascontiguousarray(FX_t, dtype=np.float32)
@@ -185,9 +190,15 @@ def regulator_order(FP_t, FX_t, sky_valid_indices):
     if FP_t.ndim != 2 or FX_t.shape != FP_t.shape:
         raise ValueError("FP/FX must both be (n_sky, n_ifo)")
     out = np.empty(valid.size, dtype=np.int32)
-    rc = load().pgw_regulator_order(FP_t.ctypes.data, FX_t.ctypes.data, FP_t.shape[1],
-                                    FP_t.shape[0], valid.ctypes.data, valid.size,
-                                    out.ctypes.data)
+    L = load()
+    if gamma_regulator is not None and hasattr(L, "pgw_regulator_order_lpt"):
+        rc = L.pgw_regulator_order_lpt(FP_t.ctypes.data, FX_t.ctypes.data, FP_t.shape[1],
+                                       FP_t.shape[0], valid.ctypes.data, valid.size,
+                                       float(gamma_regulator), out.ctypes.data)
+    else:
+        rc = L.pgw_regulator_order(FP_t.ctypes.data, FX_t.ctypes.data, FP_t.shape[1],
+                                   FP_t.shape[0], valid.ctypes.data, valid.size,
+                                   out.ctypes.data)
     check(rc, "regulator_order")
     return out
 

@@ -60,7 +60,7 @@ class SkyTables:
                else np.asarray(sky_valid_indices))
         order, n_tuples = _lib.sky_order(ml_h, v_h)
         host = (lambda x: x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x))
-        reg_order = _lib.regulator_order(host(FP_t), host(FX_t), v_h)
+        reg_order = _lib.regulator_order(host(FP_t), host(FX_t), v_h, gamma_regulator)
         return cls(FP=dv.to_device(FP_t, torch.float32), FX=dv.to_device(FX_t, torch.float32),
                    ml=dv.to_device(ml, torch.int32),
                    valid=dv.to_device(sky_valid_indices, torch.int64),

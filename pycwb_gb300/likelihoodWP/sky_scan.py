@@ -67,20 +67,21 @@ def _sky_order_device(ml, sky_valid_indices, device):
 _reg_order_cache = {}
 
 
-def _reg_order_device(FP, FX, sky_valid_indices, device):
-    """Regulator order (pgw_regulator_order), cached per (FP, FX, valid)
-    like the scan order: it orders work only, never changes a result."""
+def _reg_order_device(FP, FX, sky_valid_indices, device, gamma_regulator=None):
+    """Regulator order (pgw_regulator_order, or with gamma_regulator its
+    longest-tiles-first grouping), cached per (FP, FX, valid, gamma) like the
+    scan order: it orders work only, never changes a result."""
     def ident(x):
         if isinstance(x, torch.Tensor):
             return ("t", x.data_ptr(), tuple(x.shape))
         a = np.asarray(x)
         return ("n", id(x), a.__array_interface__["data"][0], a.shape)
-    key = (ident(FP), ident(FX), ident(sky_valid_indices))
+    key = (ident(FP), ident(FX), ident(sky_valid_indices), gamma_regulator)
     hit = _reg_order_cache.get(key)
     if hit is not None:
         return hit
     host = (lambda x: x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x))
-    order = _lib.regulator_order(host(FP), host(FX), host(sky_valid_indices))
+    order = _lib.regulator_order(host(FP), host(FX), host(sky_valid_indices), gamma_regulator)
     t = torch.from_numpy(order).to(device)
     if len(_reg_order_cache) > 16:
         _reg_order_cache.clear()
@@ -194,7 +195,8 @@ def sky_loop(n_ifo, n_pix, n_sky, FP, FX, rms, td00, td90, ml, REG0, gamma_regul
     mld = dv.to_device(ml, torch.int32)
     valid = _valid(sky_valid_indices, n_sky)
     order = _sky_order_device(ml, sky_valid_indices, FPd.device) if sky_order else None
-    rorder = _reg_order_device(FP, FX, sky_valid_indices, FPd.device) if sky_order else None
+    rorder = (_reg_order_device(FP, FX, sky_valid_indices, FPd.device, float(gamma_regulator))
+              if sky_order else None)
     ws = dv.workspace(L.pgw_workspace_bytes(n_ifo, n_delay, n_pix, 1))
     with torch.cuda.stream(s):
         stats = torch.empty((N_STATS, n_sky), dtype=torch.float32, device=FPd.device)

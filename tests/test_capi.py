@@ -160,3 +160,30 @@ def test_probability_and_pixel_arrays_reject_bad_arguments_on_the_host():
     p = ctypes.cast(buf, ctypes.c_void_p)
     assert L.pgw_skystat_pixel_arrays(3, 10, p, 64, p, p, None) != 0
     assert "workspace" in L.pgw_last_error().decode()
+
+
+def test_lpt_regulator_order_groups_the_sorted_directions():
+    """pgw_regulator_order_lpt: a permutation made of the sorted order's
+    groups of 32, the group where the key crosses the threshold first and
+    then outward."""
+    import numpy as np
+    from pycwb_gb300 import _lib, sky
+    try:
+        _lib.build()
+    except (RuntimeError, FileNotFoundError) as e:
+        pytest.skip(f"nvcc unavailable: {e}")
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(["L1", "H1", "V1"], "L1", 512.0, 20,
+                                                    healpix_order=3)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    valid = np.arange(FP_t.shape[0], dtype=np.int64)
+    plain = _lib.regulator_order(FP_t, FX_t, valid)
+    for gamma in (0.05, 0.2, 0.5, 3.0):
+        lpt = _lib.regulator_order(FP_t, FX_t, valid, gamma)
+        assert sorted(lpt.tolist()) == list(range(valid.size))
+        groups = [tuple(plain[g:g + 32]) for g in range(0, valid.size, 32)]
+        got = [tuple(lpt[g:g + 32]) for g in range(0, valid.size, 32)]
+        assert sorted(got) == sorted(groups)
+        # distances from the first group taken never decrease
+        idx = [groups.index(g) for g in got]
+        d = [abs(i - idx[0]) for i in idx]
+        assert all(d[k] <= d[k + 1] for k in range(len(d) - 1))
