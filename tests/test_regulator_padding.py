@@ -9,7 +9,8 @@ which sends the direction to the exact pass: still the reference's result,
 but slow).  This checks, with the fast pass's float32 expressions and
 flush-to-zero, that no direction of the HEALPix-7 sky for L1/H1/V1 (and of
 the HEALPix-5 sky for 2 and 4 detectors) gets such a denominator, and that
-the padding pixel adds exactly 0 to NI and |F_0|^2 to SF.
+the padding pixel adds exactly 0 to NI.  A second test checks the bound of
+the fp sum that the conditioning test and the early-fail bound use.
 """
 
 import numpy as np
@@ -55,6 +56,32 @@ def test_padding_pixel_adds_zero_for_every_direction(ifos, order):
     term, fp, den, Ad = _pad_term(FP_t, FX_t)
     assert np.all(np.isfinite(den)) and np.all(den >= TINY), "a padding pixel would give 0/0"
     assert np.all(term == 0)                    # NI unchanged
-    # SF gains fp = |F_0|^2 (up to rounding): more cautious, never less
+    # a rank-one Gram matrix: fp = |F_0|^2 up to rounding
     np.testing.assert_allclose(fp, Ad, rtol=1e-6)
     assert Ad.min() > 1e-6                      # far from the flush-to-zero range
+
+
+def test_fp_sum_bound_covers_the_running_sum():
+    """The conditioning test NI >= 1e-5 sum(fp) and the early-fail bound take
+    SF = sum_i |F_i|^2 W_i (W_i the cluster's total weight of detector i) in
+    place of the running sum of fp over the pixels seen: since
+    fp = (AP + nn) / 2 <= AP = sum_i w_i |F_i|^2, SF bounds that sum after any
+    number of pixels, so both tests only become more cautious."""
+    from pycwb_gb300 import sky
+    from pycwb_gb300.synthetic import make_cluster
+    ifos = ["L1", "H1", "V1"]
+    ml, FP, FX = sky.compute_sky_delay_and_patterns(ifos, "L1", 512.0, 20, healpix_order=4)
+    FP_t, FX_t = FP.T.astype(np.float32).copy(), FX.T.astype(np.float32).copy()
+    rng = np.random.default_rng(11)
+    for P in (1, 20, 300):
+        _, _, rms, _ = make_cluster(rng, ml, FP_t, FX_t, P, 20, 20.0)
+        w = rms.astype(np.float64) ** 2                      # (P, I)
+        Fp, Fx = FP_t.astype(np.float64), FX_t.astype(np.float64)
+        Ad, Cd, Sd = Fp * Fp + Fx * Fx, Fp * Fp - Fx * Fx, 2 * Fp * Fx
+        AP, co, si = w @ Ad.T, w @ Cd.T, w @ Sd.T            # (P, n_sky)
+        fp = 0.5 * (AP + np.sqrt(co * co + si * si))
+        running = np.cumsum(fp, axis=0)                      # after each pixel
+        # the kernel's float32 bound from the float32 totals
+        W = w.sum(axis=0).astype(np.float32)
+        SF = (Ad.astype(np.float32) * W[None, :]).sum(axis=1, dtype=np.float32)
+        assert np.all(SF.astype(np.float64) >= running.max(axis=0) * (1 - 1e-6))
