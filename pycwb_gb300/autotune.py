@@ -58,22 +58,34 @@ def _load_cache():
 
 
 def _store(key, shape, timings):
+    """Add one entry to the cache file: written to a file of this process
+    and renamed over the cache, so that concurrent tuners never leave a torn
+    file; without a writable cache the shape is simply measured again next
+    time."""
     with _lock:
         cache = _load_cache()
         cache[key] = {"shape": list(shape.key()), "timings_ms": timings}
+        tmp = f"{CACHE_PATH}.{os.getpid()}.tmp"
         try:
             os.makedirs(os.path.dirname(CACHE_PATH), exist_ok=True)
+            with open(tmp, "w") as f:
+                json.dump(cache, f, indent=1)
+            os.replace(tmp, CACHE_PATH)
         except OSError:
-            return                     # no writable cache: the shape is re-measured next time
-        tmp = CACHE_PATH + ".tmp"
-        with open(tmp, "w") as f:
-            json.dump(cache, f, indent=1)
-        os.replace(tmp, CACHE_PATH)
+            try:
+                os.remove(tmp)
+            except OSError:
+                pass
 
 
 def cached_shape(key):
+    """The cached shape of a problem class, or None (also for an entry the
+    cache holds in another form)."""
     ent = _load_cache().get(key)
-    return None if ent is None else _lib.TileShape(*ent["shape"])
+    try:
+        return None if ent is None else _lib.TileShape(*[int(v) for v in ent["shape"]])
+    except (KeyError, TypeError, ValueError):
+        return None
 
 
 def time_shape(loop, shape, reps=2):
